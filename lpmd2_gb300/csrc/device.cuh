@@ -1,0 +1,204 @@
+// device.cuh -- device-side data layout and helpers shared by the libgbmd kernels.
+//
+// Layout in HBM (one ensemble = one or many independent systems, atoms of a system
+// contiguous, each system cell-sorted):
+//   x,y,z / vx,vy,vz / ax,ay,az   FP64 structure-of-arrays master state, slot order
+//   g64 (double4_32a)                 FP64 gather copy (x, y, z, type) for the FP64 force path
+//   g32 (float4)                  position relative to the centre of the atom's home cell
+//                                 (FP32) + type bits: the coalesced 16-byte gather of the
+//                                 mixed path; differences of these offsets plus a per-pair
+//                                 cell shift give r_ij without FP32 absolute-position loss
+//   nl (uint32)                   Verlet list, column-major per system: entry k of local atom
+//                                 i at nl_base + k*natoms + i; low 25 bits = local j, high 7
+//                                 bits = cell-shift code (kx,ky,kz in -2..2)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "engine.h"
+
+namespace gbmd {
+
+constexpr int TILE = 128;          // atoms per tile = threads per block of the per-atom kernels
+constexpr int THERMO_LEN = 22;
+constexpr int PART_D = 16;         // FP64 per-tile partial sums
+constexpr int PART_I = 12;         // int64 fixed-point per-tile partial sums (mixed path)
+constexpr int CODE_SHIFT = 25;
+constexpr unsigned LOCAL_MASK = (1u << CODE_SHIFT) - 1u;
+constexpr int MAX_SYSTEM_ATOMS = (1 << CODE_SHIFT);
+constexpr double FIX_F = 4294967296.0;      // 2^32: force fixed-point scale (eV/A)
+constexpr double FIX_E = 4294967296.0;      // 2^32: energy/virial/stress fixed-point scale (eV)
+constexpr double FIX_RHO = 4294967296.0;    // 2^32: EAM density fixed-point scale
+
+// Per-atom flag bits (GBMD_FLAG_FIXEDVEL / GBMD_FLAG_FIXEDPOS of gbmd.h)
+constexpr unsigned char FLAG_FIXEDVEL = 1;
+constexpr unsigned char FLAG_FIXEDPOS = 2;
+
+// Error bits in SysState::error
+constexpr int ERR_OUTSIDE = 1;     // atom far outside the box / NaN position
+constexpr int ERR_LIST = 2;        // neighbour list capacity exceeded
+constexpr int ERR_FIXED = 4;       // fixed-point range exceeded
+constexpr int ERR_CELL = 8;        // cell occupancy beyond the sort capacity
+
+// Per-tile partial-sum slots (FP64)
+enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX = 13 };
+// Per-tile partial-sum slots (int64, mixed path)
+enum { PI_EPAIR = 0, PI_VIR = 1, PI_STRESS = 2 };
+
+struct SysDev {
+  long long atom_base;
+  int natoms;
+  int tile_base, ntiles;
+  int mode;             // NbMode
+  double L[3], Lh[3];   // box, 0.5*box
+  // binning grid (list grid for NB_LIST, the reference grid for NB_CELLS)
+  int n[3];
+  int cell_base, ncells;
+  int stencil_r;        // list stencil radius in cells (1 or 2)
+  int lc_side;          // reference stencil side (NB_CELLS)
+  double d[3];          // cell edge
+  float df[3];
+  float rlist2f;        // (cutoff + skin)^2 with a conservative margin
+  double thresh2;       // rebuild when a displacement^2 exceeds this
+  long long nl_base;
+  int rebuild_policy;
+  int each;
+  int kind_cm;          // CmKind
+  int nfree;            // atoms without fixedvel/fixedpos (Temperature's denominator)
+};
+
+struct SysState {
+  unsigned int maxdisp2;   // float bits of the largest displacement^2 since the last rebuild
+  int need_rebuild;
+  int force_rebuild;
+  int max_count;
+  int error;
+  int pad0;
+  long long rebuilds;
+  long long ucalls;        // emulated UpdateCell calls (verletlist "each")
+  long long step;
+  unsigned long long rechecks;
+};
+
+struct Dev {
+  long long N;
+  double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
+  double *mass, *fm;
+  int *type, *tag, *sysid;
+  unsigned char* flags;
+  double4_32a* g64;
+  float4* g32;
+  int* home;
+  float4* ref;
+  unsigned* nl;
+  int* ncount;
+  int maxnb;
+  int *cstart, *ccnt, *ccount, *ccursor, *acell, *perm;
+  // permutation scratch
+  double* sdbl;   // 11*N doubles
+  int* sint;      // 4*N ints
+  unsigned char* sflags;
+  // EAM
+  double *rho, *phi;
+  float* phif;
+  // multi-potential accumulation
+  long long* facc;   // 3*N fixed point
+  double* dacc;      // 3*N FP64
+  // reductions
+  double* tile_d;
+  long long* tile_i;
+  const SysDev* sysd;
+  SysState* sst;
+  const int* tile_sys;
+  const int* tile_first;
+  const int* tile_count;
+  double* thermo_last;
+  double* thermo_log;
+  int log_cap;
+  int has_flags;
+};
+
+// ---------------------------------------------------------------------------------------------
+// FP64 helpers in the reference's rounding (no fused multiply-add anywhere)
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// One axis of OrthogonalCell::Displacement (liblpmd/lpmd/orthogonalcell.h:131-149).
+__device__ __forceinline__ double ref_wrap(double d, double L, double Lh) {
+  if (d >= Lh) return dsub(d, L);
+  if (d < -Lh) return dadd(d, L);
+  return d;
+}
+
+// Vector::SquareModule (liblpmd/lpmd/vector.h:107): (x*x + y*y) + z*z.
+__device__ __forceinline__ double ref_sq(double x, double y, double z) {
+  return dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z));
+}
+
+// One axis of OrthogonalCell::FittedInside (liblpmd/lpmd/orthogonalcell.h:102-114).
+__device__ __forceinline__ double ref_fitted(double v, double L) {
+  if (v < 0.0 || v > L) v = dsub(v, dmul(L, floor(ddiv(v, L))));
+  return v;
+}
+
+// WrapAround (plugins/linkedcell.cc:9-15).
+__device__ __forceinline__ int wrap_around(int i, int n) {
+  if (i < 0)
+    i += ((-i / n) + 1) * n;
+  else if (i > n - 1)
+    i -= (i / n) * n;
+  return i;
+}
+
+// Cell coordinate of LinkedCell::UpdateCell (plugins/linkedcell.cc:249-253):
+// WrapAround(int(floor(n * (x / L))), n).  ok=false for NaN / absurdly far positions.
+__device__ __forceinline__ int ref_cell_coord(double x, double L, int n, bool& ok) {
+  double t = floor(dmul((double)n, ddiv(x, L)));
+  if (!(t > -1.0e9 && t < 1.0e9)) {
+    ok = false;
+    return 0;
+  }
+  return wrap_around((int)t, n);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of NV values per thread; thread 0 gets the totals in out[].
+template <typename T, int NV>
+__device__ __forceinline__ void block_sum(T (&v)[NV], T* out) {
+  __shared__ T sh[TILE / 32][NV];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    T s = warp_sum(v[k]);
+    if (lane == 0) sh[w][k] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      T s = sh[0][k];
+      for (int q = 1; q < TILE / 32; ++q) s += sh[q][k];
+      out[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ long long to_fixed(float v, float scale) { return __float2ll_rn(v * scale); }
+
+}  // namespace gbmd

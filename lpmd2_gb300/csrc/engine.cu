@@ -1,0 +1,1215 @@
+// engine.cu -- host runtime of libgbmd: device memory of an ensemble of independent systems,
+// configuration of the neighbour machinery, and the step pipeline (direct launches or CUDA
+// graphs whose list rebuild sits behind a device-decided conditional node).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+
+#include "forces.cuh"
+
+namespace gbmd {
+
+namespace {
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(5, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+#define CK(x) ck((x), #x)
+
+// Automatic subdivision of LinkedCell, plugins/linkedcell.cc:146-204 (one axis).
+int lc_auto_n(double len, double cutoff) {
+  double fnn = (cutoff / 2.5);
+  int n = 1;
+  for (;;) {
+    double previo = std::fabs(len / n - fnn);
+    n++;
+    double actual = std::fabs(len / n - fnn);
+    if (actual < 1E-3) break;
+    if (actual > previo) {
+      n--;
+      break;
+    }
+  }
+  if ((n % 2) != 0) n--;
+  return n;
+}
+
+inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// Layout kernels
+// ------------------------------------------------------------------------------------------
+
+__global__ void k_init_layout(Dev D, int s, long long base, int n, int cell_base) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  long long i = base + k;
+  D.sysid[i] = s;
+  D.tag[i] = k;
+  D.home[i] = cell_base;
+}
+
+// Writes caller-order (tag-indexed) interleaved host data into the slot-ordered SoA arrays.
+__global__ void k_set_atoms(Dev D, long long base, int n, const double* pos, const double* vel,
+                            const double* acc, const int* Z, const double* mass) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  long long i = base + k;
+  int t = D.tag[i];
+  if (pos) {
+    D.x[i] = pos[3 * t];
+    D.y[i] = pos[3 * t + 1];
+    D.z[i] = pos[3 * t + 2];
+  }
+  if (vel) {
+    D.vx[i] = vel[3 * t];
+    D.vy[i] = vel[3 * t + 1];
+    D.vz[i] = vel[3 * t + 2];
+  }
+  if (acc) {
+    D.ax[i] = acc[3 * t];
+    D.ay[i] = acc[3 * t + 1];
+    D.az[i] = acc[3 * t + 2];
+  }
+  if (Z) D.type[i] = Z[t];
+  if (mass) {
+    D.mass[i] = mass[t];
+    D.fm[i] = ddiv(0.00964853, mass[t]);  // forcefactor / Mass(), pairpotential.cc:62
+  }
+  D.g64[i] = make_double4_32a(D.x[i], D.y[i], D.z[i], (double)D.type[i]);
+}
+
+__global__ void k_set_flags(Dev D, long long base, int n, const unsigned char* flags) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  long long i = base + k;
+  D.flags[i] = flags ? flags[D.tag[i]] : 0;
+}
+
+__global__ void k_get_atoms(Dev D, long long base, int n, double* pos, double* vel, double* acc) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  long long i = base + k;
+  int t = D.tag[i];
+  if (pos) {
+    pos[3 * t] = D.x[i];
+    pos[3 * t + 1] = D.y[i];
+    pos[3 * t + 2] = D.z[i];
+  }
+  if (vel) {
+    vel[3 * t] = D.vx[i];
+    vel[3 * t + 1] = D.vy[i];
+    vel[3 * t + 2] = D.vz[i];
+  }
+  if (acc) {
+    acc[3 * t] = D.ax[i];
+    acc[3 * t + 1] = D.ay[i];
+    acc[3 * t + 2] = D.az[i];
+  }
+}
+
+// Neighbour export: the pairs the force kernels would use, by original index.
+// half: 0 full, 1 keep j < i (LinkedCell), 2 keep j > i (VerletList / MinimumImage).
+template <int NB, int MIXED>
+__global__ void k_export(Dev D, int s, double rc2, float rc2_lo, float rc2_hi, int half, long long* counts,
+                         const long long* offsets, long long* idx) {
+  __shared__ float4 shifts[125];
+  const SysDev& S = D.sysd[s];
+  if (MIXED) load_shifts(S, shifts);
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.natoms) return;
+  long long i = S.atom_base + k;
+  const int ti = D.tag[i];
+  long long cnt = 0;
+  long long o = offsets ? offsets[ti] : 0;
+  const float4 gi = D.g32[i];
+  const double4_32a pi = D.g64[i];
+  for_each_candidate<NB>(D, S, i, [&](long long j, unsigned code) {
+    bool in;
+    if (MIXED) {
+      const float4 gj = D.g32[j];
+      const float4 sh = shifts[code];
+      float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      float r2 = dx * dx + dy * dy + dz * dz;
+      in = r2 < rc2_lo || (r2 < rc2_hi && exact_inside(D, S, i, j, rc2));
+    } else {
+      const double4_32a pj = D.g64[j];
+      double dx = ref_wrap(dsub(pj.x, pi.x), S.L[0], S.Lh[0]);
+      double dy = ref_wrap(dsub(pj.y, pi.y), S.L[1], S.Lh[1]);
+      double dz = ref_wrap(dsub(pj.z, pi.z), S.L[2], S.Lh[2]);
+      in = ref_sq(dx, dy, dz) < rc2;
+    }
+    const int tj = D.tag[j];
+    if (half == 1 && tj > ti) in = false;
+    if (half == 2 && tj < ti) in = false;
+    if (in) {
+      if (idx) idx[o + cnt] = tj;
+      ++cnt;
+    }
+  });
+  if (counts) counts[ti] = cnt;
+}
+
+__global__ void k_cells_out(Dev D, int s, long long* cell, long long* order) {
+  const SysDev& S = D.sysd[s];
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.natoms) return;
+  long long i = S.atom_base + k;
+  cell[D.tag[i]] = D.home[i] - S.cell_base;
+  order[k] = D.tag[i];
+}
+
+__global__ void k_clear_state(Dev D, int nsys) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  D.sst[s].force_rebuild = 1;
+  D.sst[s].maxdisp2 = 0u;
+  D.sst[s].max_count = 0;
+  D.sst[s].error = 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Engine implementation
+// ------------------------------------------------------------------------------------------
+
+struct Engine::Impl {
+  int device = 0;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  int nsys = 0;
+  std::vector<int64_t> natoms;
+  std::vector<std::array<double, 3>> cells;
+  std::vector<long long> atom_base;
+  long long N = 0;
+
+  CellManagerCfg cm;
+  bool have_cm = false;
+  std::vector<PotParams> pots;
+  IntegratorCfg integ;
+  bool have_integ = false;
+  int precision = 0;
+
+  // options
+  double opt_skin = -1.0;
+  int graph_block = 10;
+  int graph_mode = 2;  // 0 direct, 1 captured, 2 captured with conditional rebuild
+  int stencil_r = 1;
+  int log_cap = 1024;
+
+  std::vector<SysDev> sysd;
+  std::vector<int> tile_sys, tile_first, tile_count;
+  int ntiles = 0;
+  int total_cells = 0;
+  bool any_list = false;
+
+  Dev D{};
+  SysDev* d_sysd = nullptr;
+  SysState* d_sst = nullptr;
+  int *d_tile_sys = nullptr, *d_tile_first = nullptr, *d_tile_count = nullptr;
+  std::vector<void*> allocs;
+  std::vector<void*> cell_allocs;
+  size_t bytes = 0, cell_bytes = 0;
+  bool configured = false, forces_valid = false, initialized = false, flags_any = false;
+  Stats st;
+
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int gsteps = 0;
+  std::map<int, long long> read_from;  // next thermo-log step to hand out, per system
+  int pending_ucalls = 0;              // UpdateCell calls owed to SetCellManager
+
+  // kernel timing with CUDA events on the simulation's stream (direct launches only)
+  enum { T_FORCE = 0, T_DRIFT = 1, T_REBUILD = 2 };
+  int time_kernels = 0;
+  bool capturing = false;
+  struct Mark {
+    cudaEvent_t a, b;
+    int cls;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t open_event[3] = {nullptr, nullptr, nullptr};
+
+  bool timing() const { return time_kernels && !capturing; }
+  cudaEvent_t get_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    return e;
+  }
+  void mark_begin(cudaStream_t s, int cls) {
+    if (!timing()) return;
+    open_event[cls] = get_event();
+    CK(cudaEventRecord(open_event[cls], s));
+  }
+  void mark_end(cudaStream_t s, int cls) {
+    if (!timing() || !open_event[cls]) return;
+    cudaEvent_t e = get_event();
+    CK(cudaEventRecord(e, s));
+    marks.push_back({open_event[cls], e, cls});
+    open_event[cls] = nullptr;
+  }
+  // Called after the stream was synchronised.
+  void collect_marks() {
+    for (const auto& m : marks) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) {
+        if (m.cls == T_FORCE) {
+          st.force_ms += ms;
+          st.force_launches++;
+        } else if (m.cls == T_DRIFT) {
+          st.drift_ms += ms;
+          st.drift_launches++;
+        } else {
+          st.rebuild_ms += ms;
+          st.rebuild_launches++;
+        }
+      }
+      cudaGetLastError();
+      event_pool.push_back(m.a);
+      event_pool.push_back(m.b);
+    }
+    marks.clear();
+  }
+
+  template <class T>
+  T* alloc(size_t n, bool cellpool = false) {
+    void* p = nullptr;
+    size_t b = sizeof(T) * (n ? n : 1);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(6, "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    CK(cudaMemsetAsync(p, 0, b, stream));
+    (cellpool ? cell_allocs : allocs).push_back(p);
+    (cellpool ? cell_bytes : bytes) += b;
+    return (T*)p;
+  }
+
+  void free_cells() {
+    for (void* p : cell_allocs) cudaFree(p);
+    cell_allocs.clear();
+    cell_bytes = 0;
+  }
+
+  void drop_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+    gsteps = 0;
+  }
+
+  void launched(int n = 1) { st.kernel_launches += n; }
+
+  void check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(5, std::string("kernel launch (") + what + "): " + cudaGetErrorString(e));
+  }
+
+  // --------------------------------------------------------------------------------------
+  void setup(int dev, const std::vector<int64_t>& na, const std::vector<std::array<double, 3>>& cl) {
+    device = dev;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+      cudaGetLastError();
+      throw Error(5, "no CUDA device available: libgbmd runs only on the GPU");
+    }
+    if (dev < 0 || dev >= count) throw Error(1, "device index out of range");
+    CK(cudaSetDevice(dev));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    natoms = na;
+    cells = cl;
+    nsys = (int)na.size();
+    if (nsys <= 0) throw Error(1, "at least one system is required");
+    atom_base.resize(nsys);
+    long long b = 0;
+    for (int s = 0; s < nsys; ++s) {
+      if (na[s] < 0 || na[s] >= MAX_SYSTEM_ATOMS)
+        throw Error(1, "atoms per system must be in [0, " + std::to_string(MAX_SYSTEM_ATOMS) + ")");
+      for (int q = 0; q < 3; ++q)
+        if (!(cl[s][q] > 0.0)) throw Error(1, "cell lengths must be positive");
+      atom_base[s] = b;
+      b += na[s];
+    }
+    N = b;
+    // tiles
+    for (int s = 0; s < nsys; ++s) {
+      for (long long k = 0; k < na[s]; k += TILE) {
+        tile_sys.push_back(s);
+        tile_first.push_back((int)(atom_base[s] + k));
+        tile_count.push_back((int)std::min<long long>(TILE, na[s] - k));
+      }
+    }
+    ntiles = (int)tile_sys.size();
+    sysd.resize(nsys);
+    int tb = 0;
+    for (int s = 0; s < nsys; ++s) {
+      SysDev& S = sysd[s];
+      std::memset(&S, 0, sizeof(S));
+      S.atom_base = atom_base[s];
+      S.natoms = (int)na[s];
+      S.tile_base = tb;
+      S.ntiles = (int)((na[s] + TILE - 1) / TILE);
+      tb += S.ntiles;
+      for (int q = 0; q < 3; ++q) {
+        S.L[q] = cl[s][q];
+        S.Lh[q] = 0.5 * cl[s][q];
+      }
+      S.n[0] = S.n[1] = S.n[2] = 1;
+      S.ncells = 1;
+      S.nfree = S.natoms;
+      S.each = 1;
+    }
+    // per-atom arrays
+    const size_t n = (size_t)N;
+    D.N = N;
+    double* st9 = alloc<double>(9 * n);
+    D.x = st9;
+    D.y = st9 + n;
+    D.z = st9 + 2 * n;
+    D.vx = st9 + 3 * n;
+    D.vy = st9 + 4 * n;
+    D.vz = st9 + 5 * n;
+    D.ax = st9 + 6 * n;
+    D.ay = st9 + 7 * n;
+    D.az = st9 + 8 * n;
+    D.mass = alloc<double>(n);
+    D.fm = alloc<double>(n);
+    D.type = alloc<int>(n);
+    D.tag = alloc<int>(n);
+    D.sysid = alloc<int>(n);
+    D.flags = alloc<unsigned char>(n);
+    D.g64 = alloc<double4_32a>(n);
+    D.g32 = alloc<float4>(n);
+    D.home = alloc<int>(n);
+    D.ref = alloc<float4>(n);
+    D.acell = alloc<int>(n);
+    D.perm = alloc<int>(n);
+    D.sdbl = alloc<double>(11 * n);
+    D.sint = alloc<int>(4 * n);
+    D.sflags = alloc<unsigned char>(n);
+    D.ncount = alloc<int>(n);
+    D.rho = alloc<double>(n);
+    D.phi = alloc<double>(n);
+    D.phif = alloc<float>(n);
+    D.facc = alloc<long long>(3 * n);
+    D.dacc = alloc<double>(3 * n);
+    D.tile_d = alloc<double>((size_t)ntiles * PART_D);
+    D.tile_i = alloc<long long>((size_t)ntiles * PART_I);
+    D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
+    D.log_cap = log_cap;
+    D.thermo_log = alloc<double>((size_t)nsys * log_cap * THERMO_LEN);
+    d_sysd = alloc<SysDev>(nsys);
+    d_sst = alloc<SysState>(nsys);
+    d_tile_sys = alloc<int>(ntiles);
+    d_tile_first = alloc<int>(ntiles);
+    d_tile_count = alloc<int>(ntiles);
+    CK(cudaMemcpyAsync(d_tile_sys, tile_sys.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tile_first, tile_first.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tile_count, tile_count.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, stream));
+    D.sysd = d_sysd;
+    D.sst = d_sst;
+    D.tile_sys = d_tile_sys;
+    D.tile_first = d_tile_first;
+    D.tile_count = d_tile_count;
+    upload_sysd();
+    for (int s = 0; s < nsys; ++s)
+      if (na[s] > 0) {
+        k_init_layout<<<nblocks(na[s], 256), 256, 0, stream>>>(D, s, atom_base[s], (int)na[s], 0);
+        launched();
+      }
+    check_launch("init");
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  void upload_sysd() {
+    CK(cudaMemcpyAsync(d_sysd, sysd.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, stream));
+  }
+
+  ~Impl() {
+    if (device >= 0) cudaSetDevice(device);
+    drop_graph();
+    if (stream) cudaStreamSynchronize(stream);
+    for (const auto& m : marks) {
+      cudaEventDestroy(m.a);
+      cudaEventDestroy(m.b);
+    }
+    for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+    for (void* p : allocs) cudaFree(p);
+    free_cells();
+    if (stream) cudaStreamDestroy(stream);
+    if (stream2) cudaStreamDestroy(stream2);
+  }
+
+  // --------------------------------------------------------------------------------------
+  // Configuration of the neighbour machinery
+  // --------------------------------------------------------------------------------------
+
+  double max_cutoff() const {
+    double rc = 0.0;
+    for (const auto& p : pots) rc = std::max(rc, p.cutoff);
+    return rc;
+  }
+
+  void configure() {
+    if (!have_cm) throw Error(4, "MissingComponent: cellmanager");
+    if (pots.empty()) throw Error(4, "MissingComponent: potential");
+    drop_graph();
+    const double rc = max_cutoff();
+    total_cells = 0;
+    any_list = false;
+    double max_expect = 0.0;
+    for (int s = 0; s < nsys; ++s) {
+      SysDev& S = sysd[s];
+      const double* L = S.L;
+      S.kind_cm = cm.kind;
+      S.rebuild_policy = REBUILD_SKIN;
+      S.each = 1;
+      S.stencil_r = stencil_r;
+      S.lc_side = 1;
+      int mode = NB_LIST;
+      double rl = 0.0;
+      if (cm.kind == CM_MINIMUMIMAGE) {
+        mode = NB_ALLPAIRS;
+      } else if (cm.kind == CM_LINKEDCELL) {
+        int n[3] = {cm.nx, cm.ny, cm.nz};
+        if (cm.mode_auto)
+          for (int q = 0; q < 3; ++q) n[q] = lc_auto_n(L[q], cm.cutoff);
+        if (n[0] <= 0 || n[1] <= 0 || n[2] <= 0)
+          throw Error(1, "linkedcell: nx, ny and nz must be positive (or mode auto)");
+        double d = L[0] / (double)n[0];
+        if (L[1] / (double)n[1] < d) d = L[1] / (double)n[1];
+        if (L[2] / (double)n[2] < d) d = L[2] / (double)n[2];
+        int side = (int)std::ceil((cm.cutoff / d) - 0.5);
+        bool complete = side >= 1;
+        for (int q = 0; q < 3; ++q) {
+          if (n[q] < 2 * side + 1) complete = false;
+          if ((double)side * (L[q] / (double)n[q]) < rc) complete = false;
+        }
+        double skin = opt_skin >= 0 ? opt_skin : (cm.skin >= 0 ? cm.skin : 0.1 * rc);
+        rl = rc + skin;
+        bool list_ok = rl < 0.5 * std::min(L[0], std::min(L[1], L[2])) && skin > 0.0;
+        if ((cm.compat || !complete || !list_ok) && precision == PREC_FP64) {
+          mode = NB_CELLS;
+          for (int q = 0; q < 3; ++q) S.n[q] = n[q];
+          S.lc_side = side < 0 ? 0 : side;
+        } else {
+          mode = NB_LIST;
+        }
+      } else {  // verletlist
+        if (std::fabs(cm.cutoff) < 1E-10) throw Error(3, "verletlist: No cutoff was defined");
+        if (cm.skin >= 0 || opt_skin >= 0) {
+          double skin = opt_skin >= 0 ? opt_skin : cm.skin;
+          rl = std::max(cm.cutoff, rc) + skin;
+          S.rebuild_policy = cm.rebuild;
+        } else {
+          rl = 1.08 * cm.cutoff;  // extcut, plugins/verletlist.cc:24-25
+          S.rebuild_policy = REBUILD_BOTH;
+        }
+        if (!(rl > rc))
+          throw Error(3, "verletlist: the list cutoff must exceed the potential cutoff");
+        S.each = (int)std::max<int64_t>(1, cm.each);
+        if (!(rl < 0.5 * std::min(L[0], std::min(L[1], L[2])))) mode = NB_ALLPAIRS;
+      }
+      if (mode == NB_ALLPAIRS && precision == PREC_MIXED)
+        throw Error(1, "mixed precision needs every box edge longer than 2*(cutoff+skin)");
+      S.mode = mode;
+      if (mode == NB_LIST) {
+        any_list = true;
+        for (int q = 0; q < 3; ++q) {
+          S.n[q] = std::max(1, (int)std::floor(L[q] * stencil_r / rl));
+          if (S.n[q] > 1024) S.n[q] = 1024;
+        }
+        S.rlist2f = (float)(rl * rl * (1.0 + 1e-5));
+        double sk = rl - rc;
+        S.thresh2 = 0.25 * sk * sk * (1.0 - 1e-4);
+        double V = L[0] * L[1] * L[2];
+        double expect = 4.18879 * rl * rl * rl * (double)S.natoms / V;
+        max_expect = std::max(max_expect, expect);
+      } else if (mode == NB_ALLPAIRS) {
+        S.n[0] = S.n[1] = S.n[2] = 1;
+      }
+      for (int q = 0; q < 3; ++q) {
+        S.d[q] = L[q] / (double)S.n[q];
+        S.df[q] = (float)S.d[q];
+      }
+      S.ncells = S.n[0] * S.n[1] * S.n[2];
+      S.cell_base = total_cells;
+      total_cells += S.ncells;
+      if (s == 0) {
+        st.neighbor_mode = mode;
+        st.list_radius = rl;
+        for (int q = 0; q < 3; ++q) st.cell_grid[q] = S.n[q];
+      }
+    }
+    for (int s = 1; s < nsys; ++s)
+      if (sysd[s].mode != sysd[0].mode)
+        throw Error(1, "every system of a batch must use the same neighbour mode (box too small for a Verlet list?)");
+    // cell arrays and neighbour list
+    free_cells();
+    D.cstart = alloc<int>(total_cells, true);
+    D.ccnt = alloc<int>(total_cells, true);
+    D.ccount = alloc<int>(total_cells, true);
+    D.ccursor = alloc<int>(total_cells, true);
+    int maxnb = 0;
+    if (any_list) {
+      maxnb = (int)std::ceil(max_expect * 1.35) + 32;
+      maxnb = (maxnb + 7) & ~7;
+    }
+    alloc_list(maxnb);
+    upload_sysd();
+    k_clear_state<<<nblocks(nsys, 128), 128, 0, stream>>>(D, nsys);
+    launched();
+    check_launch("clear");
+    configured = true;
+    forces_valid = false;
+  }
+
+  void alloc_list(int maxnb) {
+    D.maxnb = maxnb;
+    st.list_capacity = maxnb;
+    if (maxnb > 0) {
+      long long nb = 0;
+      for (int s = 0; s < nsys; ++s) {
+        sysd[s].nl_base = nb;
+        nb += (long long)sysd[s].natoms * maxnb;
+      }
+      D.nl = alloc<unsigned>((size_t)nb, true);
+    } else {
+      D.nl = nullptr;
+    }
+  }
+
+  // --------------------------------------------------------------------------------------
+  // Launch sequences
+  // --------------------------------------------------------------------------------------
+
+  void launch_decide(cudaStream_t s, int ucall_inc, int force_all, cudaGraphConditionalHandle h, int use_cond) {
+    k_decide<<<1, 256, 0, s>>>(D, nsys, ucall_inc, force_all, (unsigned long long)h, use_cond);
+    launched();
+  }
+
+  void launch_rebuild(cudaStream_t s) {
+    const unsigned nb = nblocks(N, 256);
+    mark_begin(s, T_REBUILD);
+    k_bin<<<nb, 256, 0, s>>>(D);
+    k_scan<<<nsys, 1024, 0, s>>>(D);
+    k_scatter<<<nb, 256, 0, s>>>(D);
+    int maxcells = 0;
+    for (const auto& S : sysd) maxcells = std::max(maxcells, S.ncells);
+    k_cellsort<<<dim3(nblocks(maxcells, 128), nsys), 128, 0, s>>>(D);
+    k_permute<<<nb, 256, 0, s>>>(D);
+    k_copyback<<<nb, 256, 0, s>>>(D);
+    launched(6);
+    if (any_list) {
+      k_buildlist<<<nblocks(N, 128), 128, 0, s>>>(D);
+      launched();
+    }
+    mark_end(s, T_REBUILD);
+  }
+
+  void launch_force_passes(cudaStream_t s, int epi, int count_step) {
+    const bool mixed = precision == PREC_MIXED;
+    const int np = (int)pots.size();
+    mark_begin(s, T_FORCE);
+    int first_eam = -1;
+    for (int p = 0; p < np; ++p)
+      if (pots[p].kind != POT_LJ) {
+        first_eam = p;
+        break;
+      }
+    for (int p = 0; p < np; ++p) {
+      const PotParams& P = pots[p];
+      StepParams sp;
+      sp.dt = integ.dt;
+      sp.half_dt = 0.5 * integ.dt;
+      sp.epi = epi;
+      sp.first = (p == 0);
+      sp.last = (p == np - 1);
+      sp.count_step = count_step;
+      sp.kinetic = 1;
+      const int mode = sysd[0].mode;
+      if (P.kind != POT_LJ) {
+        int first = (p == first_eam);
+        if (mixed)
+          k_eam_density<NB_LIST, 1><<<ntiles, TILE, 0, s>>>(D, P, first);
+        else if (mode == NB_LIST)
+          k_eam_density<NB_LIST, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+        else if (mode == NB_CELLS)
+          k_eam_density<NB_CELLS, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+        else
+          k_eam_density<NB_ALLPAIRS, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+        launched();
+      }
+      if (mixed) {
+        if (P.kind == POT_LJ)
+          k_force32<PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        else
+          k_force32<PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
+      } else if (mode == NB_LIST) {
+        if (P.kind == POT_LJ)
+          k_force64<NB_LIST, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        else
+          k_force64<NB_LIST, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
+      } else if (mode == NB_CELLS) {
+        if (P.kind == POT_LJ)
+          k_force64<NB_CELLS, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        else
+          k_force64<NB_CELLS, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
+      } else {
+        if (P.kind == POT_LJ)
+          k_force64<NB_ALLPAIRS, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        else
+          k_force64<NB_ALLPAIRS, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
+      }
+      launched();
+    }
+    mark_end(s, T_FORCE);
+    k_thermo<<<nsys, TILE, 0, s>>>(D, mixed ? 1 : 0, count_step);
+    launched();
+  }
+
+  void ensure_ready() {
+    if (!configured) configure();
+    CK(cudaSetDevice(device));
+  }
+
+  // Reads the per-system error words and the list statistics (synchronises the stream).
+  void check_errors() {
+    CK(cudaStreamSynchronize(stream));
+    collect_marks();
+    std::vector<SysState> hs(nsys);
+    CK(cudaMemcpy(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost));
+    int err = 0, maxc = 0;
+    long long rb = 0;
+    unsigned long long rech = 0;
+    for (const auto& x : hs) {
+      err |= x.error;
+      maxc = std::max(maxc, x.max_count);
+      rb += x.rebuilds;
+      rech += x.rechecks;
+    }
+    st.max_neighbors = maxc;
+    st.list_rebuilds = rb;
+    st.fp_guard_rechecks = (int64_t)rech;
+    if (err & ERR_OUTSIDE) throw Error(8, "RuntimeError: atom position is not finite or far outside the simulation box");
+    if (err & ERR_LIST) throw Error(7, "neighbour list capacity exceeded (maxneighbors is too small!)");
+    // VerletListCellManager throws once an atom reaches maxneighbors-1 list entries
+    // (plugins/verletlist.cc:96-97)
+    if (cm.kind == CM_VERLETLIST && maxnb_cap > 0 && maxc >= maxnb_cap - 1)
+      throw Error(3, "PluginError: verletlist: maxneighbors is too small!");
+  }
+  long long maxnb_cap = 0;
+
+  // First build: size the list from the measured maximum and rebuild if it did not fit.
+  void first_build() {
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      launch_decide(stream, attempt == 0 ? 1 + pending_ucalls : 0, 1, 0, 0);
+      launch_rebuild(stream);
+      check_launch("rebuild");
+      CK(cudaStreamSynchronize(stream));
+      std::vector<SysState> hs(nsys);
+      CK(cudaMemcpy(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost));
+      int maxc = 0, err = 0;
+      for (const auto& x : hs) {
+        maxc = std::max(maxc, x.max_count);
+        err |= x.error;
+      }
+      if (err & ERR_OUTSIDE) throw Error(8, "RuntimeError: atom position is not finite or far outside the simulation box");
+      pending_ucalls = 0;
+      if (!any_list || maxc <= D.maxnb * 0.8) return;
+      // grow: re-allocate the list with room to spare and rebuild from scratch
+      int maxnb = (int)std::ceil(maxc * 1.4) + 16;
+      maxnb = (maxnb + 7) & ~7;
+      cudaFree(D.nl);
+      cell_allocs.erase(std::find(cell_allocs.begin(), cell_allocs.end(), (void*)D.nl));
+      alloc_list(maxnb);
+      upload_sysd();
+      k_clear_state<<<nblocks(nsys, 128), 128, 0, stream>>>(D, nsys);
+      launched();
+    }
+    throw Error(7, "could not size the neighbour list");
+  }
+
+  // One force evaluation at the current positions (CombinedPotential::UpdateForces).
+  void update_forces() {
+    ensure_ready();
+    if (!forces_valid_layout) {
+      first_build();
+      forces_valid_layout = true;
+      launch_force_passes(stream, EPI_FORCES, 0);
+    } else {
+      launch_decide(stream, 1, 0, 0, 0);
+      launch_rebuild(stream);
+      launch_force_passes(stream, EPI_FORCES, 0);
+    }
+    check_launch("update_forces");
+    st.force_evaluations++;
+    check_errors();
+    forces_valid = true;
+  }
+  bool forces_valid_layout = false;
+
+  void launch_step(cudaStream_t s, int ucall_inc, bool conditional, cudaGraphConditionalHandle h) {
+    mark_begin(s, T_DRIFT);
+    k_drift<<<nblocks(N, 256), 256, 0, s>>>(D, integ.dt);
+    mark_end(s, T_DRIFT);
+    launched();
+    launch_decide(s, ucall_inc, 0, h, conditional ? 1 : 0);
+    if (!conditional) launch_rebuild(s);
+  }
+
+  void build_graph(int nsteps) {
+    drop_graph();
+    CK(cudaGraphCreate(&graph, 0));
+    bool cond = graph_mode == 2;
+    std::vector<cudaGraphConditionalHandle> handles(nsteps);
+    if (cond) {
+      for (int k = 0; k < nsteps; ++k) {
+        if (cudaGraphConditionalHandleCreate(&handles[k], graph, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+          cudaGetLastError();
+          cond = false;
+          break;
+        }
+      }
+    }
+    CK(cudaStreamBeginCaptureToGraph(stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    int64_t saved = st.kernel_launches;
+    capturing = true;
+    try {
+      for (int k = 0; k < nsteps; ++k) {
+        launch_step(stream, 2, cond, cond ? handles[k] : 0);
+        if (cond) {
+          cudaStreamCaptureStatus cs;
+          cudaGraph_t g;
+          const cudaGraphNode_t* deps = nullptr;
+          size_t ndeps = 0;
+          CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+          cudaGraphNodeParams cp = {};
+          cp.type = cudaGraphNodeTypeConditional;
+          cp.conditional.handle = handles[k];
+          cp.conditional.type = cudaGraphCondTypeIf;
+          cp.conditional.size = 1;
+          cudaGraphNode_t cnode;
+          CK(cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp));
+          cudaGraph_t body = cp.conditional.phGraph_out[0];
+          CK(cudaStreamUpdateCaptureDependencies(stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+          CK(cudaStreamBeginCaptureToGraph(stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+          launch_rebuild(stream2);
+          cudaGraph_t bout;
+          CK(cudaStreamEndCapture(stream2, &bout));
+        }
+        launch_force_passes(stream, EPI_KICK, 1);
+      }
+    } catch (...) {
+      capturing = false;
+      cudaGraph_t tmp;
+      cudaStreamEndCapture(stream, &tmp);
+      cudaGetLastError();
+      st.kernel_launches = saved;
+      drop_graph();
+      throw;
+    }
+    capturing = false;
+    cudaGraph_t out;
+    CK(cudaStreamEndCapture(stream, &out));
+    st.kernel_launches = saved;
+    CK(cudaGraphInstantiate(&gexec, graph, 0));
+    gsteps = nsteps;
+    graph_cond = cond;
+  }
+  bool graph_cond = false;
+
+  int64_t kernels_per_step_base() const {
+    int np = (int)pots.size();
+    int eam = 0;
+    for (const auto& p : pots) eam += (p.kind != POT_LJ);
+    return 2 /*drift, decide*/ + np + eam + 1 /*thermo*/;
+  }
+
+  void do_steps(int64_t nsteps) {
+    ensure_ready();
+    if (!have_integ) throw Error(4, "MissingComponent: integrator");
+    if (nsteps <= 0) return;
+    if (!forces_valid) update_forces();
+    int first_extra = 0;
+    if (!initialized) {
+      // VelocityVerlet::Initialize -> UseOldConfig -> SetCellManager: one more UpdateCell call
+      first_extra = 1;
+      initialized = true;
+    }
+    int64_t done = 0;
+    long long rb_before = st.list_rebuilds;
+    if (first_extra) {
+      launch_step(stream, 3, false, 0);
+      launch_force_passes(stream, EPI_KICK, 1);
+      check_launch("step");
+      done = 1;
+    }
+    const int gb = graph_block;
+    if (graph_mode > 0 && gb > 0) {
+      while (nsteps - done >= gb) {
+        if (!gexec || gsteps != gb) build_graph(gb);
+        CK(cudaGraphLaunch(gexec, stream));
+        st.kernel_launches += gb * kernels_per_step_base() + (graph_cond ? 0 : gb * (6 + (any_list ? 1 : 0)));
+        done += gb;
+      }
+    }
+    while (done < nsteps) {
+      launch_step(stream, 2, false, 0);
+      launch_force_passes(stream, EPI_KICK, 1);
+      check_launch("step");
+      ++done;
+    }
+    st.steps += nsteps;
+    st.force_evaluations += nsteps;
+    check_errors();
+    if (graph_cond) st.kernel_launches += (st.list_rebuilds - rb_before) * (6 + (any_list ? 1 : 0));
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// Engine API
+// ------------------------------------------------------------------------------------------
+
+Engine::Engine(int device, const std::vector<int64_t>& natoms, const std::vector<std::array<double, 3>>& cells)
+    : natoms_(natoms), d_(new Impl) {
+  try {
+    d_->setup(device, natoms, cells);
+  } catch (...) {
+    delete d_;
+    throw;
+  }
+}
+
+Engine::~Engine() { delete d_; }
+
+void Engine::set_atoms(int sys, const double* pos, const double* vel, const double* acc, const int32_t* Z,
+                       const double* mass) {
+  Impl& I = *d_;
+  CK(cudaSetDevice(I.device));
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  const int n = (int)I.natoms[sys];
+  if (n == 0) return;
+  const size_t v3 = sizeof(double) * 3 * n;
+  // one staging buffer: pos | vel | acc | mass (doubles) then Z (ints)
+  size_t tot = 3 * v3 + sizeof(double) * n + sizeof(int) * n;
+  char* stg = nullptr;
+  CK(cudaMalloc(&stg, tot));
+  try {
+    double* dp = (double*)stg;
+    double* dv = dp + 3 * n;
+    double* da = dv + 3 * n;
+    double* dm = da + 3 * n;
+    int* dz = (int*)(dm + n);
+    if (pos) CK(cudaMemcpyAsync(dp, pos, v3, cudaMemcpyHostToDevice, I.stream));
+    if (vel) CK(cudaMemcpyAsync(dv, vel, v3, cudaMemcpyHostToDevice, I.stream));
+    else CK(cudaMemsetAsync(dv, 0, v3, I.stream));
+    if (acc) CK(cudaMemcpyAsync(da, acc, v3, cudaMemcpyHostToDevice, I.stream));
+    else CK(cudaMemsetAsync(da, 0, v3, I.stream));
+    if (mass) CK(cudaMemcpyAsync(dm, mass, sizeof(double) * n, cudaMemcpyHostToDevice, I.stream));
+    if (Z) CK(cudaMemcpyAsync(dz, Z, sizeof(int) * n, cudaMemcpyHostToDevice, I.stream));
+    k_set_atoms<<<nblocks(n, 256), 256, 0, I.stream>>>(I.D, I.atom_base[sys], n, pos ? dp : nullptr, dv, da,
+                                                        Z ? dz : nullptr, mass ? dm : nullptr);
+    I.launched();
+    I.check_launch("set_atoms");
+    CK(cudaStreamSynchronize(I.stream));
+  } catch (...) {
+    cudaFree(stg);
+    throw;
+  }
+  cudaFree(stg);
+  I.forces_valid = false;
+  I.forces_valid_layout = false;
+}
+
+void Engine::set_flags(int sys, const uint8_t* flags) {
+  Impl& I = *d_;
+  CK(cudaSetDevice(I.device));
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  const int n = (int)I.natoms[sys];
+  int nfixed = 0;
+  if (flags)
+    for (int k = 0; k < n; ++k)
+      if (flags[k] & (FLAG_FIXEDVEL | FLAG_FIXEDPOS)) ++nfixed;
+  I.sysd[sys].nfree = n - nfixed;
+  if (n == 0) return;
+  unsigned char* df = nullptr;
+  CK(cudaMalloc(&df, n));
+  if (flags) CK(cudaMemcpyAsync(df, flags, n, cudaMemcpyHostToDevice, I.stream));
+  k_set_flags<<<nblocks(n, 256), 256, 0, I.stream>>>(I.D, I.atom_base[sys], n, flags ? df : nullptr);
+  I.launched();
+  CK(cudaStreamSynchronize(I.stream));
+  cudaFree(df);
+  if (nfixed) I.flags_any = true;
+  I.D.has_flags = I.flags_any ? 1 : 0;
+  I.upload_sysd();
+  I.drop_graph();
+}
+
+void Engine::get_atoms(int sys, double* pos, double* vel, double* acc) {
+  Impl& I = *d_;
+  CK(cudaSetDevice(I.device));
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  const int n = (int)I.natoms[sys];
+  if (n == 0) return;
+  const size_t v3 = sizeof(double) * 3 * n;
+  double* stg = nullptr;
+  CK(cudaMalloc(&stg, 3 * v3));
+  k_get_atoms<<<nblocks(n, 256), 256, 0, I.stream>>>(I.D, I.atom_base[sys], n, stg, stg + 3 * n, stg + 6 * n);
+  I.launched();
+  if (pos) CK(cudaMemcpyAsync(pos, stg, v3, cudaMemcpyDeviceToHost, I.stream));
+  if (vel) CK(cudaMemcpyAsync(vel, stg + 3 * n, v3, cudaMemcpyDeviceToHost, I.stream));
+  if (acc) CK(cudaMemcpyAsync(acc, stg + 6 * n, v3, cudaMemcpyDeviceToHost, I.stream));
+  cudaError_t e = cudaStreamSynchronize(I.stream);
+  cudaFree(stg);
+  ck(e, "get_atoms");
+}
+
+void Engine::set_cell_manager(const CellManagerCfg& cfg) {
+  d_->cm = cfg;
+  d_->have_cm = true;
+  d_->pending_ucalls = 1;  // Configuration::SetCellManager calls UpdateCell once
+  d_->configured = false;
+  d_->forces_valid = false;
+  d_->forces_valid_layout = false;
+}
+
+void Engine::add_potential(const PotParams& p) {
+  if (d_->pots.size() >= 8) throw Error(1, "at most 8 potentials");
+  d_->pots.push_back(p);
+  d_->configured = false;
+  d_->forces_valid = false;
+  d_->forces_valid_layout = false;
+}
+
+void Engine::set_integrator(const IntegratorCfg& cfg) {
+  if (!(cfg.dt > 0.0) || !std::isfinite(cfg.dt)) throw Error(1, "velocityverlet: dt must be positive");
+  d_->integ = cfg;
+  d_->have_integ = true;
+  d_->drop_graph();
+}
+
+void Engine::set_precision(int precision) {
+  if (precision != PREC_FP64 && precision != PREC_MIXED)
+    throw Error(1, "unknown precision");
+  if (precision != d_->precision) {
+    d_->precision = precision;
+    d_->configured = false;
+    d_->forces_valid = false;
+    d_->forces_valid_layout = false;
+  }
+}
+
+void Engine::set_option(const std::string& key, const std::string& value) {
+  Impl& I = *d_;
+  char* end = nullptr;
+  double v = std::strtod(value.c_str(), &end);
+  if (end == value.c_str()) throw Error(1, "option " + key + ": not a number: " + value);
+  if (key == "maxneighbors_cap") {
+    I.maxnb_cap = (long long)v;
+    return;
+  }
+  if (key == "time_kernels") {
+    I.time_kernels = (int)v;
+    return;
+  }
+  if (key == "skin") {
+    I.opt_skin = v;
+  } else if (key == "graph_block") {
+    I.graph_block = (int)v;
+  } else if (key == "graph_mode") {
+    I.graph_mode = (int)v;
+  } else if (key == "cell_scale" || key == "stencil") {
+    if ((int)v != 1 && (int)v != 2) throw Error(1, "cell_scale must be 1 or 2");
+    I.stencil_r = (int)v;
+  } else {
+    throw Error(1, "unknown option " + key);
+  }
+  I.configured = false;
+  I.forces_valid = false;
+  I.forces_valid_layout = false;
+  I.drop_graph();
+}
+
+void Engine::update_forces() { d_->update_forces(); }
+void Engine::do_steps(int64_t nsteps) { d_->do_steps(nsteps); }
+void Engine::synchronize() {
+  CK(cudaSetDevice(d_->device));
+  CK(cudaStreamSynchronize(d_->stream));
+}
+
+void Engine::thermo(int sys, double* out22) {
+  Impl& I = *d_;
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  CK(cudaSetDevice(I.device));
+  CK(cudaMemcpyAsync(out22, I.D.thermo_last + (size_t)sys * THERMO_LEN, sizeof(double) * THERMO_LEN,
+                     cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+}
+
+int64_t Engine::thermo_log(int sys, double* out, int64_t cap) {
+  Impl& I = *d_;
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  CK(cudaSetDevice(I.device));
+  std::vector<double> all((size_t)I.log_cap * THERMO_LEN);
+  CK(cudaMemcpy(all.data(), I.D.thermo_log + (size_t)sys * I.log_cap * THERMO_LEN, sizeof(double) * all.size(),
+                cudaMemcpyDeviceToHost));
+  SysState hs;
+  CK(cudaMemcpy(&hs, I.d_sst + sys, sizeof(SysState), cudaMemcpyDeviceToHost));
+  long long last = hs.step;
+  long long first = std::max<long long>(1, last - I.log_cap + 1);
+  if (!I.read_from.count(sys)) I.read_from[sys] = 1;
+  first = std::max(first, I.read_from[sys]);
+  int64_t c = 0;
+  for (long long stp = first; stp <= last && c < cap; ++stp, ++c)
+    std::memcpy(out + c * THERMO_LEN, all.data() + (stp % I.log_cap) * THERMO_LEN, sizeof(double) * THERMO_LEN);
+  I.read_from[sys] = first + c;
+  return c;
+}
+
+Stats Engine::stats() {
+  Impl& I = *d_;
+  if (I.configured) I.check_errors();
+  Stats s = I.st;
+  s.device_bytes = (int64_t)(I.bytes + I.cell_bytes);
+  return s;
+}
+
+void* Engine::stream() const { return (void*)d_->stream; }
+
+void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t* idx, int64_t cap, int64_t* total) {
+  Impl& I = *d_;
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  I.ensure_ready();
+  if (!I.forces_valid) I.update_forces();
+  const SysDev& S = I.sysd[sys];
+  const int n = S.natoms;
+  if (S.mode == NB_LIST) {
+    double rl = std::sqrt((double)S.rlist2f / (1.0 + 1e-5));
+    if (rcut > rl * (1.0 - 1e-9))
+      throw Error(1, "rcut exceeds the neighbour-list radius (cutoff + skin)");
+  }
+  int half = 0;
+  if (!full) half = (I.cm.kind == CM_LINKEDCELL) ? 1 : 2;
+  const double rc2 = rcut * rcut;
+  const float lo = (float)(rc2 * (1.0 - 8e-6)), hi = (float)(rc2 * (1.0 + 8e-6));
+  const bool mixed = I.precision == PREC_MIXED;
+  long long *dc = nullptr, *doff = nullptr, *didx = nullptr;
+  CK(cudaMalloc(&dc, sizeof(long long) * std::max(n, 1)));
+  CK(cudaMalloc(&doff, sizeof(long long) * std::max(n, 1)));
+  auto launch = [&](long long* cnt, const long long* off, long long* ix) {
+    const unsigned nb = nblocks(n, 128);
+    if (n == 0) return;
+    if (S.mode == NB_LIST) {
+      if (mixed)
+        k_export<NB_LIST, 1><<<nb, 128, 0, I.stream>>>(I.D, sys, rc2, lo, hi, half, cnt, off, ix);
+      else
+        k_export<NB_LIST, 0><<<nb, 128, 0, I.stream>>>(I.D, sys, rc2, lo, hi, half, cnt, off, ix);
+    } else if (S.mode == NB_CELLS) {
+      k_export<NB_CELLS, 0><<<nb, 128, 0, I.stream>>>(I.D, sys, rc2, lo, hi, half, cnt, off, ix);
+    } else {
+      k_export<NB_ALLPAIRS, 0><<<nb, 128, 0, I.stream>>>(I.D, sys, rc2, lo, hi, half, cnt, off, ix);
+    }
+    I.launched();
+    I.check_launch("export");
+  };
+  try {
+    launch(dc, nullptr, nullptr);
+    std::vector<long long> hc(n), ho(n);
+    CK(cudaMemcpyAsync(hc.data(), dc, sizeof(long long) * n, cudaMemcpyDeviceToHost, I.stream));
+    CK(cudaStreamSynchronize(I.stream));
+    long long t = 0;
+    for (int k = 0; k < n; ++k) {
+      ho[k] = t;
+      t += hc[k];
+    }
+    if (counts)
+      for (int k = 0; k < n; ++k) counts[k] = hc[k];
+    if (total) *total = t;
+    if (idx && t > 0) {
+      if (cap < t) throw Error(9, "neighbour index buffer too small");
+      CK(cudaMalloc(&didx, sizeof(long long) * t));
+      CK(cudaMemcpyAsync(doff, ho.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, I.stream));
+      launch(nullptr, doff, didx);
+      CK(cudaMemcpyAsync(idx, didx, sizeof(long long) * t, cudaMemcpyDeviceToHost, I.stream));
+      CK(cudaStreamSynchronize(I.stream));
+    }
+  } catch (...) {
+    cudaFree(dc);
+    cudaFree(doff);
+    cudaFree(didx);
+    throw;
+  }
+  cudaFree(dc);
+  cudaFree(doff);
+  cudaFree(didx);
+}
+
+void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* order) {
+  Impl& I = *d_;
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  for (int q = 0; q < 3; ++q)
+    if (n[q] <= 0) throw Error(1, "cell grid must be positive");
+  I.ensure_ready();
+  // Bin and sort on the requested grid with the rebuild kernels, then restore the config.
+  std::vector<SysDev> saved = I.sysd;
+  I.free_cells();
+  int total = 0;
+  for (int s = 0; s < I.nsys; ++s) {
+    SysDev& S = I.sysd[s];
+    S.mode = NB_CELLS;
+    for (int q = 0; q < 3; ++q) S.n[q] = n[q];
+    S.ncells = n[0] * n[1] * n[2];
+    S.cell_base = total;
+    total += S.ncells;
+  }
+  I.D.cstart = I.alloc<int>(total, true);
+  I.D.ccnt = I.alloc<int>(total, true);
+  I.D.ccount = I.alloc<int>(total, true);
+  I.D.ccursor = I.alloc<int>(total, true);
+  I.D.nl = nullptr;
+  bool any_list = I.any_list;
+  I.any_list = false;
+  I.upload_sysd();
+  I.launch_decide(I.stream, 0, 1, 0, 0);
+  I.launch_rebuild(I.stream);
+  I.any_list = any_list;
+  const int na = I.sysd[sys].natoms;
+  long long *dc = nullptr, *dord = nullptr;
+  CK(cudaMalloc(&dc, sizeof(long long) * std::max(na, 1)));
+  CK(cudaMalloc(&dord, sizeof(long long) * std::max(na, 1)));
+  if (na > 0) k_cells_out<<<nblocks(na, 128), 128, 0, I.stream>>>(I.D, sys, dc, dord);
+  I.check_launch("cell_sort");
+  std::vector<long long> hc(na), ho(na);
+  CK(cudaMemcpyAsync(hc.data(), dc, sizeof(long long) * na, cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaMemcpyAsync(ho.data(), dord, sizeof(long long) * na, cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  cudaFree(dc);
+  cudaFree(dord);
+  for (int k = 0; k < na; ++k) {
+    if (cell) cell[k] = hc[k];
+    if (order) order[k] = ho[k];
+  }
+  I.sysd = saved;
+  I.configured = false;
+  I.forces_valid = false;
+  I.forces_valid_layout = false;
+}
+
+}  // namespace gbmd

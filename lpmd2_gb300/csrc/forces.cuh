@@ -1,0 +1,418 @@
+// forces.cuh -- force, density and thermo kernels (one thread per atom, one block per tile of
+// 128 atoms of one system; every atom gathers over its full neighbour list, so no atomics and
+// every sum has a fixed order).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace gbmd {
+
+enum PotClass { PC_PAIR = 0, PC_EAM = 1 };
+
+// Visits the candidate neighbours j of atom i under neighbour mode NB (compile-time).
+template <int NB, class F>
+__device__ __forceinline__ void for_each_candidate(const Dev& D, const SysDev& S, long long i, F&& f) {
+  if (NB == NB_LIST) {
+    const int na = S.natoms;
+    const unsigned* L = D.nl + S.nl_base + (i - S.atom_base);
+    const int cnt = D.ncount[i];
+    for (int k = 0; k < cnt; ++k) {
+      unsigned e = __ldg(L + (long long)k * na);
+      f(S.atom_base + (long long)(e & LOCAL_MASK), e >> CODE_SHIFT);
+    }
+  } else if (NB == NB_CELLS) {
+    // The reference stencil of LinkedCell (plugins/linkedcell.cc:221-240), duplicates included.
+    const int h = D.home[i] - S.cell_base;
+    const int cx = h % S.n[0], cy = (h / S.n[0]) % S.n[1], cz = h / (S.n[0] * S.n[1]);
+    const int sd = S.lc_side;
+    for (int dz = -sd; dz <= sd; ++dz) {
+      int zc = wrap_around(cz + dz, S.n[2]);
+      for (int dy = -sd; dy <= sd; ++dy) {
+        int yc = wrap_around(cy + dy, S.n[1]);
+        for (int dx = -sd; dx <= sd; ++dx) {
+          int xc = wrap_around(cx + dx, S.n[0]);
+          int g = S.cell_base + (zc * S.n[1] + yc) * S.n[0] + xc;
+          int b = D.cstart[g], e = b + D.ccnt[g];
+          for (int j = b; j < e; ++j)
+            if (j != i) f((long long)j, 0u);
+        }
+      }
+    }
+  } else {
+    for (long long j = S.atom_base; j < S.atom_base + S.natoms; ++j)
+      if (j != i) f(j, 0u);
+  }
+}
+
+// Exact FP64 reference cutoff test of pair (i, j) from the master positions.
+__device__ __forceinline__ bool exact_inside(const Dev& D, const SysDev& S, long long i, long long j, double rc2) {
+  double dx = ref_wrap(dsub(D.x[j], D.x[i]), S.L[0], S.Lh[0]);
+  double dy = ref_wrap(dsub(D.y[j], D.y[i]), S.L[1], S.Lh[1]);
+  double dz = ref_wrap(dsub(D.z[j], D.z[i]), S.L[2], S.Lh[2]);
+  return ref_sq(dx, dy, dz) < rc2;
+}
+
+// Loads the cell-shift table (k * cell edge, k in -2..2 per axis) of system S into shared memory.
+__device__ __forceinline__ void load_shifts(const SysDev& S, float4* sh) {
+  for (int c = threadIdx.x; c < 125; c += blockDim.x) {
+    int kx = c % 5 - 2, ky = (c / 5) % 5 - 2, kz = c / 25 - 2;
+    sh[c] = make_float4((float)kx * S.df[0], (float)ky * S.df[1], (float)kz * S.df[2], 0.0f);
+  }
+  __syncthreads();
+}
+
+// Epilogue shared by the force kernels: turns the total force on atom i into its acceleration
+// (a = F * forcefactor/m, liblpmd/simulation/pairpotential.cc:62), applies fixedvel, and for
+// EPI_KICK advances the velocity: v = v + (0.5*dt) * (a_old + a) (plugins/velocityverlet.cc:73-74).
+// Returns the kinetic terms of the updated velocity.
+__device__ __forceinline__ void finish_atom(const Dev& D, long long i, double Fx, double Fy, double Fz,
+                                            const StepParams& sp, double& ke, double& px, double& py, double& pz) {
+  const double fm = D.fm[i];
+  double ax = dmul(Fx, fm), ay = dmul(Fy, fm), az = dmul(Fz, fm);
+  unsigned char fl = D.has_flags ? D.flags[i] : 0;
+  if (fl & FLAG_FIXEDVEL) ax = ay = az = 0.0;
+  double vx = D.vx[i], vy = D.vy[i], vz = D.vz[i];
+  if (sp.epi == EPI_KICK && !(fl & FLAG_FIXEDPOS)) {
+    vx = dadd(vx, dmul(sp.half_dt, dadd(D.ax[i], ax)));
+    vy = dadd(vy, dmul(sp.half_dt, dadd(D.ay[i], ay)));
+    vz = dadd(vz, dmul(sp.half_dt, dadd(D.az[i], az)));
+    D.vx[i] = vx;
+    D.vy[i] = vy;
+    D.vz[i] = vz;
+  }
+  D.ax[i] = ax;
+  D.ay[i] = ay;
+  D.az[i] = az;
+  ke = 0.0;
+  px = py = pz = 0.0;
+  // KineticEnergy/Momentum skip tagged atoms (liblpmd/lpmd/properties.h:22-37,64-81)
+  if (sp.kinetic && !(fl & (FLAG_FIXEDVEL | FLAG_FIXEDPOS))) {
+    const double m = D.mass[i];
+    ke = dmul(dmul(0.5, m), ref_sq(vx, vy, vz));
+    px = dmul(vx, m);
+    py = dmul(vy, m);
+    pz = dmul(vz, m);
+  }
+}
+
+// Writes the tile's FP64 partials (slots [lo, hi) of the 16) with overwrite or accumulate.
+__device__ __forceinline__ void store_tile_d(const Dev& D, int tile, const double* v, int lo, int hi, bool first) {
+  double* t = D.tile_d + (long long)tile * PART_D;
+  for (int k = lo; k < hi; ++k) t[k] = first ? v[k] : t[k] + v[k];
+}
+
+// ------------------------------------------------------------------------------------------
+// FP64 force pass: pair (LJ) or EAM force.
+// ------------------------------------------------------------------------------------------
+
+template <int NB, int PC>
+__global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams sp) {
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
+  const SysDev& S = D.sysd[s];
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  const bool active = (int)threadIdx.x < D.tile_count[tile];
+  double fx = 0.0, fy = 0.0, fz = 0.0, ep = 0.0, vir = 0.0;
+  double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0, szz = 0.0;
+  if (active) {
+    const double4_32a pi = D.g64[i];
+    const int ti = (int)pi.w;
+    const double phi_i = (PC == PC_EAM) ? D.phi[i] : 0.0;
+    for_each_candidate<NB>(D, S, i, [&](long long j, unsigned) {
+      const double4_32a pj = D.g64[j];
+      double dx = ref_wrap(dsub(pj.x, pi.x), S.L[0], S.Lh[0]);
+      double dy = ref_wrap(dsub(pj.y, pi.y), S.L[1], S.Lh[1]);
+      double dz = ref_wrap(dsub(pj.z, pi.z), S.L[2], S.Lh[2]);
+      double r2 = ref_sq(dx, dy, dz);
+      if (r2 < P.rc2 && applies_to(P.spc_sum, ti, (int)pj.w)) {
+        double g, e;
+        if (PC == PC_PAIR) {
+          lj_pair64(P, r2, g, e);
+        } else {
+          double r = sqrt(r2);
+          double sc;
+          eam_pair64(P, r, phi_i, D.phi[j], sc, e);
+          g = ddiv(sc, r);
+        }
+        fx += g * dx;
+        fy += g * dy;
+        fz += g * dz;
+        ep += e;
+        vir -= g * r2;
+        sxx -= g * dx * dx;
+        sxy -= g * dx * dy;
+        sxz -= g * dx * dz;
+        syy -= g * dy * dy;
+        syz -= g * dy * dz;
+        szz -= g * dz * dz;
+      }
+    });
+  }
+  double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+  if (active) {
+    long long N = D.N;
+    if (!sp.first) {
+      fx += D.dacc[i];
+      fy += D.dacc[N + i];
+      fz += D.dacc[2 * N + i];
+    }
+    if (sp.last) {
+      finish_atom(D, i, fx, fy, fz, sp, ke, px, py, pz);
+    } else {
+      D.dacc[i] = fx;
+      D.dacc[N + i] = fy;
+      D.dacc[2 * N + i] = fz;
+    }
+  }
+  // the full list counts each pair twice: halve energy, virial and stress
+  double v[13] = {0.5 * ep, 0.5 * vir, 0.5 * sxx, 0.5 * sxy, 0.5 * sxz, 0.5 * sxy, 0.5 * syy,
+                  0.5 * syz, 0.5 * sxz, 0.5 * syz, 0.5 * szz, ke, 0.0};
+  double tot[13];
+  block_sum<double, 13>(v, tot);
+  if (threadIdx.x == 0) {
+    double out[PART_D] = {0};
+    out[PD_EPAIR] = tot[0];
+    out[PD_VIR] = tot[1];
+    for (int k = 0; k < 9; ++k) out[PD_STRESS + k] = tot[2 + k];
+    store_tile_d(D, tile, out, PD_EPAIR, PD_EPAIR + 1, sp.first);
+    store_tile_d(D, tile, out, PD_VIR, PD_STRESS + 9, sp.first);
+  }
+  if (sp.last) {
+    double k4[4] = {ke, px, py, pz};
+    double kt[4];
+    block_sum<double, 4>(k4, kt);
+    if (threadIdx.x == 0) {
+      double* t = D.tile_d + (long long)tile * PART_D;
+      t[PD_KE] = kt[0];
+      t[PD_PX] = kt[1];
+      t[PD_PX + 1] = kt[2];
+      t[PD_PX + 2] = kt[3];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Mixed force pass: FP32 pair maths, int64 fixed-point force sums, FP64 cutoff test inside a
+// guard band around rc^2 so the set of interacting pairs is the FP64 reference's.
+// ------------------------------------------------------------------------------------------
+
+template <int PC>
+__global__ void __launch_bounds__(TILE) k_force32(Dev D, PotParams P, StepParams sp) {
+  __shared__ float4 shifts[125];
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
+  const SysDev& S = D.sysd[s];
+  load_shifts(S, shifts);
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  const bool active = (int)threadIdx.x < D.tile_count[tile];
+  long long qx = 0, qy = 0, qz = 0;
+  float ep = 0.f, vir = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  const float rc2_lo = P.f[12], rc2_hi = P.f[13];
+  const float fscale = (float)FIX_F;
+  unsigned long long rechecks = 0;
+  if (active) {
+    const float4 gi = D.g32[i];
+    const int ti = __float_as_int(gi.w);
+    const float phi_i = (PC == PC_EAM) ? D.phif[i] : 0.f;
+    for_each_candidate<NB_LIST>(D, S, i, [&](long long j, unsigned code) {
+      const float4 gj = D.g32[j];
+      const float4 sh = shifts[code];
+      float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < rc2_hi) {
+        bool in = r2 < rc2_lo;
+        if (!in) {
+          in = exact_inside(D, S, i, j, P.rc2);
+          ++rechecks;
+        }
+        if (in && applies_to(P.spc_sum, ti, __float_as_int(gj.w))) {
+          float g, e;
+          if (PC == PC_PAIR) {
+            lj_pair32(P, __frcp_rn(r2), g, e);
+          } else {
+            eam_pair32(P, r2, phi_i, D.phif[j], g, e);
+          }
+          float gs = g * fscale;
+          qx += __float2ll_rn(gs * dx);
+          qy += __float2ll_rn(gs * dy);
+          qz += __float2ll_rn(gs * dz);
+          ep += e;
+          vir -= g * r2;
+          sxx -= g * dx * dx;
+          sxy -= g * dx * dy;
+          sxz -= g * dx * dz;
+          syy -= g * dy * dy;
+          syz -= g * dy * dz;
+          szz -= g * dz * dz;
+        }
+      }
+    });
+  }
+  double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+  if (active) {
+    const long long N = D.N;
+    if (!sp.first) {
+      qx += D.facc[i];
+      qy += D.facc[N + i];
+      qz += D.facc[2 * N + i];
+    }
+    if (sp.last) {
+      const double inv = 1.0 / FIX_F;
+      finish_atom(D, i, (double)qx * inv, (double)qy * inv, (double)qz * inv, sp, ke, px, py, pz);
+    } else {
+      D.facc[i] = qx;
+      D.facc[N + i] = qy;
+      D.facc[2 * N + i] = qz;
+    }
+    if (rechecks) atomicAdd(&D.sst[s].rechecks, rechecks);
+  }
+  // per-atom energy/virial/stress (halved: full list) to int64 fixed point, exact block sums
+  const float es = (float)(0.5 * FIX_E);
+  long long v[11] = {__float2ll_rn(ep * es), __float2ll_rn(vir * es), __float2ll_rn(sxx * es),
+                     __float2ll_rn(sxy * es), __float2ll_rn(sxz * es), __float2ll_rn(sxy * es),
+                     __float2ll_rn(syy * es), __float2ll_rn(syz * es), __float2ll_rn(sxz * es),
+                     __float2ll_rn(syz * es), __float2ll_rn(szz * es)};
+  long long tot[11];
+  block_sum<long long, 11>(v, tot);
+  if (threadIdx.x == 0) {
+    long long* t = D.tile_i + (long long)tile * PART_I;
+    for (int k = 0; k < 11; ++k) t[k] = sp.first ? tot[k] : t[k] + tot[k];
+  }
+  if (sp.last) {
+    double k4[4] = {ke, px, py, pz};
+    double kt[4];
+    block_sum<double, 4>(k4, kt);
+    if (threadIdx.x == 0) {
+      double* t = D.tile_d + (long long)tile * PART_D;
+      t[PD_KE] = kt[0];
+      t[PD_PX] = kt[1];
+      t[PD_PX + 1] = kt[2];
+      t[PD_PX + 2] = kt[3];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// EAM density pass + embedding (FP64 embedding in both precisions).
+// ------------------------------------------------------------------------------------------
+
+template <int NB, int MIXED>
+__global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int first) {
+  __shared__ float4 shifts[125];
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
+  const SysDev& S = D.sysd[s];
+  if (MIXED) load_shifts(S, shifts);
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  const bool active = (int)threadIdx.x < D.tile_count[tile];
+  double F = 0.0;
+  if (active) {
+    double rho = 0.0;
+    if (MIXED) {
+      long long q = 0;
+      const float4 gi = D.g32[i];
+      const float rc2_lo = P.f[12], rc2_hi = P.f[13];
+      const float scale = (float)FIX_RHO;
+      for_each_candidate<NB_LIST>(D, S, i, [&](long long j, unsigned code) {
+        const float4 gj = D.g32[j];
+        const float4 sh = shifts[code];
+        float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+        float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < rc2_hi) {
+          bool in = r2 < rc2_lo;
+          if (!in) in = exact_inside(D, S, i, j, P.rc2);
+          if (in) q += __float2ll_rn(eam_rho32(P, r2) * scale);
+        }
+      });
+      rho = (double)q * (1.0 / FIX_RHO);
+    } else {
+      const double4_32a pi = D.g64[i];
+      for_each_candidate<NB>(D, S, i, [&](long long j, unsigned) {
+        const double4_32a pj = D.g64[j];
+        double dx = ref_wrap(dsub(pj.x, pi.x), S.L[0], S.Lh[0]);
+        double dy = ref_wrap(dsub(pj.y, pi.y), S.L[1], S.Lh[1]);
+        double dz = ref_wrap(dsub(pj.z, pi.z), S.L[2], S.Lh[2]);
+        double r2 = ref_sq(dx, dy, dz);
+        if (r2 < P.rc2) rho += eam_rho64(P, sqrt(r2));
+      });
+    }
+    double phi;
+    eam_embed64(P, rho, F, phi);
+    D.rho[i] = rho;
+    D.phi[i] = phi;
+    D.phif[i] = (float)phi;
+  }
+  double v[1] = {F};
+  double t[1];
+  block_sum<double, 1>(v, t);
+  if (threadIdx.x == 0) {
+    double* td = D.tile_d + (long long)tile * PART_D;
+    td[PD_EEMBED] = first ? t[0] : td[PD_EEMBED] + t[0];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Thermo record per system (one block per system; fixed-order reductions).
+// ------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_step) {
+  const int s = blockIdx.x;
+  const SysDev& S = D.sysd[s];
+  SysState& st = D.sst[s];
+  double v[PART_D];
+  long long q[PART_I];
+  for (int k = 0; k < PART_D; ++k) v[k] = 0.0;
+  for (int k = 0; k < PART_I; ++k) q[k] = 0;
+  for (int t = threadIdx.x; t < S.ntiles; t += blockDim.x) {
+    const double* td = D.tile_d + (long long)(S.tile_base + t) * PART_D;
+    for (int k = 0; k < PART_D; ++k) v[k] += td[k];
+    if (mixed) {
+      const long long* ti = D.tile_i + (long long)(S.tile_base + t) * PART_I;
+      for (int k = 0; k < PART_I; ++k) q[k] += ti[k];
+    }
+  }
+  double tot[PART_D];
+  long long qt[PART_I];
+  block_sum<double, PART_D>(v, tot);
+  block_sum<long long, PART_I>(q, qt);
+  if (threadIdx.x == 0) {
+    double epair = tot[PD_EPAIR], vir = tot[PD_VIR];
+    double stress[9];
+    for (int k = 0; k < 9; ++k) stress[k] = tot[PD_STRESS + k];
+    if (mixed) {
+      const double inv = 1.0 / FIX_E;
+      epair = (double)qt[PI_EPAIR] * inv;
+      vir = (double)qt[PI_VIR] * inv;
+      for (int k = 0; k < 9; ++k) stress[k] = (double)qt[PI_STRESS + k] * inv;
+    }
+    if (count_step) st.step += 1;
+    const double KIN2EV = 103.64269, KB = 8.6173422E-05, PRESSF = 160217.65;
+    double epot = epair + tot[PD_EEMBED];
+    double kin = dmul(tot[PD_KE], KIN2EV);
+    double temp = (S.natoms == 0) ? 0.0 : ddiv(dmul(2.0 / 3.0, kin), dmul(KB, (double)S.nfree));
+    double vol = dmul(dmul(S.L[0], S.L[1]), S.L[2]);
+    double r[THERMO_LEN];
+    r[0] = (double)st.step;
+    r[1] = epot;
+    r[2] = kin;
+    r[3] = epot + kin;
+    r[4] = temp;
+    r[5] = vir;
+    r[6] = tot[PD_PX];
+    r[7] = tot[PD_PX + 1];
+    r[8] = tot[PD_PX + 2];
+    r[9] = vol;
+    r[10] = dmul(dmul(ddiv(PRESSF, vol), 1.0 / 3.0), vir);
+    r[11] = dmul(dmul(ddiv(PRESSF, vol), 2.0 / 3.0), kin);
+    r[12] = dmul(ddiv(PRESSF, vol), dadd(dmul(2.0 / 3.0, kin), dmul(1.0 / 3.0, vir)));
+    for (int k = 0; k < 9; ++k) r[13 + k] = stress[k];
+    double* last = D.thermo_last + (long long)s * THERMO_LEN;
+    double* log = D.thermo_log + ((long long)s * D.log_cap + (st.step % D.log_cap)) * THERMO_LEN;
+    for (int k = 0; k < THERMO_LEN; ++k) {
+      last[k] = r[k];
+      if (count_step) log[k] = r[k];
+    }
+  }
+}
+
+}  // namespace gbmd

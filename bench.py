@@ -218,9 +218,15 @@ def main():
     ap.add_argument("--impl", default="gbmd", choices=["gbmd", "reference"])
     ap.add_argument("--melt", type=int, default=1000, help="untimed mixed steps that melt the lattice")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile", action="store_true",
+                    help="short direct-launch run of the workload for ncu (no timing, no JSON)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.profile:
+        run_profile(args)
         return
     if args.warmup < 3:
         args.warmup = 3
@@ -353,6 +359,19 @@ def main():
     if cpu:
         out["cpu_baseline"] = cpu
     print(json.dumps(out))
+
+
+def run_profile(args):
+    """The workload with direct launches only (graph_mode 0), for ncu: melt, warm up, then
+    --steps steps.  Every kernel of a step is a separate launch on the simulation's stream."""
+    w = workload()
+    sim = make_sim(w, args.precision)
+    sim.set_option("graph_mode", 0)
+    sim.update_forces()
+    sim.do_steps(args.melt + args.warmup)
+    sim.do_steps(args.steps)
+    sim.synchronize()
+    print(json.dumps({"profile": True, "natoms": w["natoms"], "steps": args.steps, **sim.stats()}))
 
 
 def kernel_times(w, device: int) -> dict:

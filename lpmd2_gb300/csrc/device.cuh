@@ -45,6 +45,9 @@ constexpr int ERR_CELL = 8;        // cell occupancy beyond the sort capacity
 enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX = 13 };
 // Per-tile partial-sum slots (int64, mixed path)
 enum { PI_EPAIR = 0, PI_VIR = 1, PI_STRESS = 2 };
+// Per-system int64 fixed-point accumulators of the mixed path (atomics from every block)
+enum { SA_EPAIR = 0, SA_VIR = 1, SA_STRESS = 2, SA_KE = 11, SA_P = 12, SA_EEMBED = 15, SA_LEN = 16 };
+constexpr double FIX_KE = 1099511627776.0;  // 2^40: kinetic energy (amu A^2/fs^2) and momentum
 
 struct SysDev {
   long long atom_base;
@@ -66,6 +69,10 @@ struct SysDev {
   int each;
   int kind_cm;          // CmKind
   int nfree;            // atoms without fixedvel/fixedpos (Temperature's denominator)
+  double vol;           // L0*L1*L2 (OrthogonalCell::Volume)
+  double pv;            // pressfactor / volume
+  double kbn;           // KBOLTZMANN * nfree
+  double ninv[3];       // n / L: binning multiplier of the Verlet-list grid
 };
 
 struct SysState {
@@ -83,7 +90,12 @@ struct SysState {
 
 struct Dev {
   long long N;
+  // positions are double-buffered: (x, y, z, g32, g64) are the positions a launch evaluates
+  // forces at; the fused drift writes the next step's positions into (xo, yo, zo, g32o, g64o)
   double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
+  double *xo, *yo, *zo;
+  float4* g32o;
+  double4_32a* g64o;
   double *mass, *fm;
   int *type, *tag, *sysid;
   unsigned char* flags;
@@ -108,6 +120,7 @@ struct Dev {
   // reductions
   double* tile_d;
   long long* tile_i;
+  unsigned long long* sys_acc;  // nsys * SA_LEN
   const SysDev* sysd;
   SysState* sst;
   const int* tile_sys;
@@ -118,6 +131,16 @@ struct Dev {
   int log_cap;
   int has_flags;
 };
+
+// Verlet-list layout: entries are stored in groups of four (16 bytes).  Group q of the local
+// atom li of system S sits at uint4 index nl_base/4 + q*natoms + li, so a warp of consecutive
+// atoms loads 512 contiguous bytes per group and each lane gets four entries per load.
+__device__ __forceinline__ const uint4* list_group(const Dev& D, const SysDev& S, int li, int q) {
+  return reinterpret_cast<const uint4*>(D.nl + S.nl_base) + (long long)q * S.natoms + li;
+}
+__device__ __forceinline__ unsigned* list_slot(const Dev& D, const SysDev& S, int li, int k) {
+  return D.nl + S.nl_base + ((long long)(k >> 2) * S.natoms + li) * 4 + (k & 3);
+}
 
 // ---------------------------------------------------------------------------------------------
 // FP64 helpers in the reference's rounding (no fused multiply-add anywhere)
@@ -166,6 +189,15 @@ __device__ __forceinline__ int ref_cell_coord(double x, double L, int n, bool& o
   return wrap_around((int)t, n);
 }
 
+__device__ __forceinline__ int list_cell_coord(double t, int n, bool& ok) {
+  double f = floor(t);
+  if (!(f > -1.0e9 && f < 1.0e9)) {
+    ok = false;
+    return 0;
+  }
+  return wrap_around((int)f, n);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Reductions
 // ---------------------------------------------------------------------------------------------
@@ -199,6 +231,57 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T* out) {
   __syncthreads();
 }
 
-__device__ __forceinline__ long long to_fixed(float v, float scale) { return __float2ll_rn(v * scale); }
+// ---------------------------------------------------------------------------------------------
+// Fixed-point accumulation on the FP32/INT pipes.
+//
+// GB300's FP64 unit (2 instructions/clock/SM) also executes every conversion to or from a
+// 64-bit type, so __float2ll_rn per pair would make the force kernel FP64-bound.  Instead a
+// scaled FP32 value y (|y| < 2^44) is split exactly as y = h*2^22 + l with integer h
+// (|h| < 2^22) and |l| <= 2^21, and both parts are rounded to integers with the classic
+// "add 1.5*2^23" trick (the integer lands in the low mantissa bits).  round(y) = h*2^22 +
+// round(l) exactly, with round-half-even, so the int64 sums are exact and order-independent.
+// ---------------------------------------------------------------------------------------------
+
+constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
+constexpr int MAGIC_BITS = 0x4B400000;
+constexpr float SPLIT = 4194304.0f;            // 2^22
+constexpr float INV_SPLIT = 2.384185791015625e-07f;  // 2^-22
+
+struct Fix {
+  int hi = 0, lo = 0;
+  __device__ __forceinline__ void add(float y) {
+    float t = fmaf(y, INV_SPLIT, MAGIC);  // MAGIC + round(y / 2^22)
+    float h = t - MAGIC;                  // exact
+    float l = fmaf(-h, SPLIT, y);         // exact, |l| <= 2^21
+    float u = l + MAGIC;                  // MAGIC + round(l)
+    hi += __float_as_int(t) - MAGIC_BITS;
+    lo += __float_as_int(u) - MAGIC_BITS;
+  }
+  // add(f * 2^32) for |f| < 2^12, with the scaling folded into the split (6 FP32/INT ops):
+  // t = M + round(f*2^10); the remainder f - h*2^-10 is exact and |.| <= 2^-11.
+  __device__ __forceinline__ void add_scaled32(float f) {
+    float t = fmaf(f, 1024.0f, MAGIC);
+    float h = t - MAGIC;
+    float r = fmaf(-h, 9.765625e-04f, f);
+    float u = fmaf(r, 4294967296.0f, MAGIC);
+    hi += __float_as_int(t) - MAGIC_BITS;
+    lo += __float_as_int(u) - MAGIC_BITS;
+  }
+  __device__ __forceinline__ long long value() const { return ((long long)hi << 22) + (long long)lo; }
+};
+
+// round(y) as int64 for one FP32 value (|y| < 2^44), FP32/INT pipes only.
+__device__ __forceinline__ long long fix64(float y) {
+  Fix f;
+  f.add(y);
+  return f.value();
+}
+
+// Approximate reciprocal (MUFU.RCP, <= 1 ulp).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 }  // namespace gbmd

@@ -220,9 +220,33 @@ struct Engine::Impl {
   bool configured = false, forces_valid = false, initialized = false, flags_any = false;
   Stats st;
 
+  // double-buffered positions: cbuf holds the committed positions of the last completed step;
+  // when pend is set, the other buffer already holds the drifted positions of the next step
+  double* Pbuf[2] = {nullptr, nullptr};
+  double4_32a* G64buf[2] = {nullptr, nullptr};
+  float4* G32buf[2] = {nullptr, nullptr};
+  int cbuf = 0;
+  bool pend = false;
+
+  // Points the launch descriptor at buffer `in` (evaluation) and 1-in (drift output).
+  void set_buffers(int in) {
+    const size_t n = (size_t)N;
+    D.x = Pbuf[in];
+    D.y = Pbuf[in] + n;
+    D.z = Pbuf[in] + 2 * n;
+    D.g64 = G64buf[in];
+    D.g32 = G32buf[in];
+    D.xo = Pbuf[1 - in];
+    D.yo = Pbuf[1 - in] + n;
+    D.zo = Pbuf[1 - in] + 2 * n;
+    D.g64o = G64buf[1 - in];
+    D.g32o = G32buf[1 - in];
+  }
+
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   int gsteps = 0;
+  int gparity = -1;  // cbuf the graph was captured for
   std::map<int, long long> read_from;  // next thermo-log step to hand out, per system
   int pending_ucalls = 0;              // UpdateCell calls owed to SetCellManager
 
@@ -311,6 +335,7 @@ struct Engine::Impl {
     gexec = nullptr;
     graph = nullptr;
     gsteps = 0;
+    gparity = -1;
   }
 
   void launched(int n = 1) { st.kernel_launches += n; }
@@ -373,29 +398,33 @@ struct Engine::Impl {
       S.n[0] = S.n[1] = S.n[2] = 1;
       S.ncells = 1;
       S.nfree = S.natoms;
+      S.vol = (cl[s][0] * cl[s][1]) * cl[s][2];
+      S.pv = 160217.65 / S.vol;  // pressfactor / Cell().Volume() (simulationbuilder.cc:86,112)
+      S.kbn = 8.6173422E-05 * (double)S.nfree;
       S.each = 1;
     }
     // per-atom arrays
     const size_t n = (size_t)N;
     D.N = N;
-    double* st9 = alloc<double>(9 * n);
-    D.x = st9;
-    D.y = st9 + n;
-    D.z = st9 + 2 * n;
-    D.vx = st9 + 3 * n;
-    D.vy = st9 + 4 * n;
-    D.vz = st9 + 5 * n;
-    D.ax = st9 + 6 * n;
-    D.ay = st9 + 7 * n;
-    D.az = st9 + 8 * n;
+    double* st6 = alloc<double>(6 * n);
+    D.vx = st6;
+    D.vy = st6 + n;
+    D.vz = st6 + 2 * n;
+    D.ax = st6 + 3 * n;
+    D.ay = st6 + 4 * n;
+    D.az = st6 + 5 * n;
+    for (int b = 0; b < 2; ++b) {
+      Pbuf[b] = alloc<double>(3 * n);
+      G64buf[b] = alloc<double4_32a>(n);
+      G32buf[b] = alloc<float4>(n);
+    }
+    set_buffers(0);
     D.mass = alloc<double>(n);
     D.fm = alloc<double>(n);
     D.type = alloc<int>(n);
     D.tag = alloc<int>(n);
     D.sysid = alloc<int>(n);
     D.flags = alloc<unsigned char>(n);
-    D.g64 = alloc<double4_32a>(n);
-    D.g32 = alloc<float4>(n);
     D.home = alloc<int>(n);
     D.ref = alloc<float4>(n);
     D.acell = alloc<int>(n);
@@ -411,6 +440,7 @@ struct Engine::Impl {
     D.dacc = alloc<double>(3 * n);
     D.tile_d = alloc<double>((size_t)ntiles * PART_D);
     D.tile_i = alloc<long long>((size_t)ntiles * PART_I);
+    D.sys_acc = alloc<unsigned long long>((size_t)nsys * SA_LEN);
     D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
     D.log_cap = log_cap;
     D.thermo_log = alloc<double>((size_t)nsys * log_cap * THERMO_LEN);
@@ -532,7 +562,9 @@ struct Engine::Impl {
       if (mode == NB_LIST) {
         any_list = true;
         for (int q = 0; q < 3; ++q) {
-          S.n[q] = std::max(1, (int)std::floor(L[q] * stencil_r / rl));
+          // cells at least (cutoff+skin)/stencil_r wide, with a 1e-4 margin that covers
+          // binning by multiplication instead of division
+          S.n[q] = std::max(1, (int)std::floor(L[q] * stencil_r / (rl * (1.0 + 1e-4))));
           if (S.n[q] > 1024) S.n[q] = 1024;
         }
         S.rlist2f = (float)(rl * rl * (1.0 + 1e-5));
@@ -549,6 +581,7 @@ struct Engine::Impl {
         S.df[q] = (float)S.d[q];
       }
       S.ncells = S.n[0] * S.n[1] * S.n[2];
+      for (int q = 0; q < 3; ++q) S.ninv[q] = (double)S.n[q] / L[q];
       S.cell_base = total_cells;
       total_cells += S.ncells;
       if (s == 0) {
@@ -612,12 +645,12 @@ struct Engine::Impl {
     k_scatter<<<nb, 256, 0, s>>>(D);
     int maxcells = 0;
     for (const auto& S : sysd) maxcells = std::max(maxcells, S.ncells);
-    k_cellsort<<<dim3(nblocks(maxcells, 128), nsys), 128, 0, s>>>(D);
+    k_cellsort<<<dim3(nblocks(maxcells, 4), nsys), 128, 0, s>>>(D);
     k_permute<<<nb, 256, 0, s>>>(D);
     k_copyback<<<nb, 256, 0, s>>>(D);
     launched(6);
     if (any_list) {
-      k_buildlist<<<nblocks(N, 128), 128, 0, s>>>(D);
+      k_buildlist<<<dim3(nblocks(maxcells, LIST_WARPS), nsys), 32 * LIST_WARPS, 0, s>>>(D);
       launched();
     }
     mark_end(s, T_REBUILD);
@@ -657,10 +690,18 @@ struct Engine::Impl {
         launched();
       }
       if (mixed) {
-        if (P.kind == POT_LJ)
-          k_force32<PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
-        else
-          k_force32<PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        const bool species = P.spc_sum >= 0;
+        if (P.kind == POT_LJ) {
+          if (species)
+            k_force32<PC_PAIR, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
+          else
+            k_force32<PC_PAIR, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        } else {
+          if (species)
+            k_force32<PC_EAM, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
+          else
+            k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
+        }
       } else if (mode == NB_LIST) {
         if (P.kind == POT_LJ)
           k_force64<NB_LIST, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
@@ -749,6 +790,7 @@ struct Engine::Impl {
   // One force evaluation at the current positions (CombinedPotential::UpdateForces).
   void update_forces() {
     ensure_ready();
+    set_buffers(cbuf);
     if (!forces_valid_layout) {
       first_build();
       forces_valid_layout = true;
@@ -762,16 +804,34 @@ struct Engine::Impl {
     st.force_evaluations++;
     check_errors();
     forces_valid = true;
+    pend = false;
   }
   bool forces_valid_layout = false;
 
-  void launch_step(cudaStream_t s, int ucall_inc, bool conditional, cudaGraphConditionalHandle h) {
+  // Stand-alone AdvancePosition from the committed positions into the other buffer.
+  void launch_drift(cudaStream_t s) {
+    set_buffers(cbuf);
     mark_begin(s, T_DRIFT);
-    k_drift<<<nblocks(N, 256), 256, 0, s>>>(D, integ.dt);
+    if (precision == PREC_MIXED)
+      k_drift<1><<<ntiles, TILE, 0, s>>>(D, integ.dt);
+    else
+      k_drift<0><<<ntiles, TILE, 0, s>>>(D, integ.dt);
     mark_end(s, T_DRIFT);
     launched();
+    pend = true;
+  }
+
+  // First half of a step: switch to the drifted buffer and decide whether to rebuild.
+  void launch_step_head(cudaStream_t s, int ucall_inc, bool conditional, cudaGraphConditionalHandle h) {
+    set_buffers(1 - cbuf);
     launch_decide(s, ucall_inc, 0, h, conditional ? 1 : 0);
     if (!conditional) launch_rebuild(s);
+  }
+
+  // Second half: fused force + kick + drift into the other buffer; commits the step.
+  void launch_step_tail(cudaStream_t s) {
+    launch_force_passes(s, EPI_KICK_DRIFT, 1);
+    cbuf = 1 - cbuf;
   }
 
   void build_graph(int nsteps) {
@@ -790,10 +850,11 @@ struct Engine::Impl {
     }
     CK(cudaStreamBeginCaptureToGraph(stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     int64_t saved = st.kernel_launches;
+    const int cbuf0 = cbuf;
     capturing = true;
     try {
       for (int k = 0; k < nsteps; ++k) {
-        launch_step(stream, 2, cond, cond ? handles[k] : 0);
+        launch_step_head(stream, 2, cond, cond ? handles[k] : 0);
         if (cond) {
           cudaStreamCaptureStatus cs;
           cudaGraph_t g;
@@ -814,10 +875,11 @@ struct Engine::Impl {
           cudaGraph_t bout;
           CK(cudaStreamEndCapture(stream2, &bout));
         }
-        launch_force_passes(stream, EPI_KICK, 1);
+        launch_step_tail(stream);
       }
     } catch (...) {
       capturing = false;
+      cbuf = cbuf0;
       cudaGraph_t tmp;
       cudaStreamEndCapture(stream, &tmp);
       cudaGetLastError();
@@ -826,11 +888,13 @@ struct Engine::Impl {
       throw;
     }
     capturing = false;
+    cbuf = cbuf0;  // capture does not execute: the buffers flip when the graph runs
     cudaGraph_t out;
     CK(cudaStreamEndCapture(stream, &out));
     st.kernel_launches = saved;
     CK(cudaGraphInstantiate(&gexec, graph, 0));
     gsteps = nsteps;
+    gparity = cbuf0;
     graph_cond = cond;
   }
   bool graph_cond = false;
@@ -839,7 +903,7 @@ struct Engine::Impl {
     int np = (int)pots.size();
     int eam = 0;
     for (const auto& p : pots) eam += (p.kind != POT_LJ);
-    return 2 /*drift, decide*/ + np + eam + 1 /*thermo*/;
+    return 1 /*decide*/ + np + eam + 1 /*thermo*/;
   }
 
   void do_steps(int64_t nsteps) {
@@ -847,6 +911,7 @@ struct Engine::Impl {
     if (!have_integ) throw Error(4, "MissingComponent: integrator");
     if (nsteps <= 0) return;
     if (!forces_valid) update_forces();
+    if (!pend) launch_drift(stream);
     int first_extra = 0;
     if (!initialized) {
       // VelocityVerlet::Initialize -> UseOldConfig -> SetCellManager: one more UpdateCell call
@@ -856,23 +921,27 @@ struct Engine::Impl {
     int64_t done = 0;
     long long rb_before = st.list_rebuilds;
     if (first_extra) {
-      launch_step(stream, 3, false, 0);
-      launch_force_passes(stream, EPI_KICK, 1);
+      launch_step_head(stream, 3, false, 0);
+      launch_step_tail(stream);
       check_launch("step");
       done = 1;
     }
     const int gb = graph_block;
     if (graph_mode > 0 && gb > 0) {
-      while (nsteps - done >= gb) {
-        if (!gexec || gsteps != gb) build_graph(gb);
+      // a block of gb steps flips the buffers gb times: keep its parity even so one graph
+      // serves every block
+      const int gbe = gb & ~1;
+      if (gbe > 0 && (cbuf != gparity || !gexec || gsteps != gbe) && nsteps - done >= gbe)
+        build_graph(gbe);
+      while (gbe > 0 && nsteps - done >= gbe && gparity == cbuf) {
         CK(cudaGraphLaunch(gexec, stream));
-        st.kernel_launches += gb * kernels_per_step_base() + (graph_cond ? 0 : gb * (6 + (any_list ? 1 : 0)));
-        done += gb;
+        st.kernel_launches += gbe * kernels_per_step_base() + (graph_cond ? 0 : gbe * (6 + (any_list ? 1 : 0)));
+        done += gbe;
       }
     }
     while (done < nsteps) {
-      launch_step(stream, 2, false, 0);
-      launch_force_passes(stream, EPI_KICK, 1);
+      launch_step_head(stream, 2, false, 0);
+      launch_step_tail(stream);
       check_launch("step");
       ++done;
     }
@@ -903,6 +972,8 @@ void Engine::set_atoms(int sys, const double* pos, const double* vel, const doub
                        const double* mass) {
   Impl& I = *d_;
   CK(cudaSetDevice(I.device));
+  I.set_buffers(I.cbuf);
+  I.pend = false;
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
   const int n = (int)I.natoms[sys];
   if (n == 0) return;
@@ -948,6 +1019,7 @@ void Engine::set_flags(int sys, const uint8_t* flags) {
     for (int k = 0; k < n; ++k)
       if (flags[k] & (FLAG_FIXEDVEL | FLAG_FIXEDPOS)) ++nfixed;
   I.sysd[sys].nfree = n - nfixed;
+  I.sysd[sys].kbn = 8.6173422E-05 * (double)(n - nfixed);
   if (n == 0) return;
   unsigned char* df = nullptr;
   CK(cudaMalloc(&df, n));
@@ -965,6 +1037,7 @@ void Engine::set_flags(int sys, const uint8_t* flags) {
 void Engine::get_atoms(int sys, double* pos, double* vel, double* acc) {
   Impl& I = *d_;
   CK(cudaSetDevice(I.device));
+  I.set_buffers(I.cbuf);
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
   const int n = (int)I.natoms[sys];
   if (n == 0) return;
@@ -1098,6 +1171,7 @@ void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t*
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
   I.ensure_ready();
   if (!I.forces_valid) I.update_forces();
+  I.set_buffers(I.cbuf);
   const SysDev& S = I.sysd[sys];
   const int n = S.natoms;
   if (S.mode == NB_LIST) {
@@ -1167,6 +1241,8 @@ void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* orde
   for (int q = 0; q < 3; ++q)
     if (n[q] <= 0) throw Error(1, "cell grid must be positive");
   I.ensure_ready();
+  I.set_buffers(I.cbuf);
+  I.pend = false;
   // Bin and sort on the requested grid with the rebuild kernels, then restore the config.
   std::vector<SysDev> saved = I.sysd;
   I.free_cells();

@@ -14,11 +14,13 @@ template <int NB, class F>
 __device__ __forceinline__ void for_each_candidate(const Dev& D, const SysDev& S, long long i, F&& f) {
   if (NB == NB_LIST) {
     const int na = S.natoms;
-    const unsigned* L = D.nl + S.nl_base + (i - S.atom_base);
+    const uint4* L = list_group(D, S, (int)(i - S.atom_base), 0);
     const int cnt = D.ncount[i];
-    for (int k = 0; k < cnt; ++k) {
-      unsigned e = __ldg(L + (long long)k * na);
-      f(S.atom_base + (long long)(e & LOCAL_MASK), e >> CODE_SHIFT);
+    for (int k = 0; k < cnt; k += 4) {
+      const uint4 e4 = __ldg(L);
+      L += na;
+      const unsigned e[4] = {e4.x, e4.y, e4.z, e4.w};
+      for (int u = 0; u < 4 && k + u < cnt; ++u) f(S.atom_base + (long long)(e[u] & LOCAL_MASK), e[u] >> CODE_SHIFT);
     }
   } else if (NB == NB_CELLS) {
     // The reference stencil of LinkedCell (plugins/linkedcell.cc:221-240), duplicates included.
@@ -52,6 +54,12 @@ __device__ __forceinline__ bool exact_inside(const Dev& D, const SysDev& S, long
   return ref_sq(dx, dy, dz) < rc2;
 }
 
+// Out-of-line copy for the hot loops: the guard-band recheck is rare (a few pairs per thousand
+// atoms), and keeping its FP64 code out of the loop body keeps the body small.
+__device__ __noinline__ bool exact_inside_cold(const Dev* D, const SysDev* S, long long i, long long j, double rc2) {
+  return exact_inside(*D, *S, i, j, rc2);
+}
+
 // Loads the cell-shift table (k * cell edge, k in -2..2 per axis) of system S into shared memory.
 __device__ __forceinline__ void load_shifts(const SysDev& S, float4* sh) {
   for (int c = threadIdx.x; c < 125; c += blockDim.x) {
@@ -62,20 +70,30 @@ __device__ __forceinline__ void load_shifts(const SysDev& S, float4* sh) {
 }
 
 // Epilogue shared by the force kernels: turns the total force on atom i into its acceleration
-// (a = F * forcefactor/m, liblpmd/simulation/pairpotential.cc:62), applies fixedvel, and for
-// EPI_KICK advances the velocity: v = v + (0.5*dt) * (a_old + a) (plugins/velocityverlet.cc:73-74).
-// Returns the kinetic terms of the updated velocity.
-__device__ __forceinline__ void finish_atom(const Dev& D, long long i, double Fx, double Fy, double Fz,
-                                            const StepParams& sp, double& ke, double& px, double& py, double& pz) {
+// (a = F * forcefactor/m, liblpmd/simulation/pairpotential.cc:62), applies fixedvel, and unless
+// EPI_FORCES advances the velocity: v = v + (0.5*dt) * (a_old + a) (plugins/velocityverlet.cc:73-74).
+// EPI_KICK_DRIFT then also advances the position for the next step (AdvancePosition) into the
+// output position buffer.  Returns the kinetic terms of the updated velocity and the squared
+// displacement since the last list build.
+template <int MIXED>
+__device__ __forceinline__ float finish_atom(const Dev& D, const SysDev& S, long long i, double Fx, double Fy,
+                                             double Fz, const StepParams& sp, double& ke, double& px, double& py,
+                                             double& pz) {
   const double fm = D.fm[i];
   double ax = dmul(Fx, fm), ay = dmul(Fy, fm), az = dmul(Fz, fm);
   unsigned char fl = D.has_flags ? D.flags[i] : 0;
   if (fl & FLAG_FIXEDVEL) ax = ay = az = 0.0;
   double vx = D.vx[i], vy = D.vy[i], vz = D.vz[i];
-  if (sp.epi == EPI_KICK && !(fl & FLAG_FIXEDPOS)) {
-    vx = dadd(vx, dmul(sp.half_dt, dadd(D.ax[i], ax)));
-    vy = dadd(vy, dmul(sp.half_dt, dadd(D.ay[i], ay)));
-    vz = dadd(vz, dmul(sp.half_dt, dadd(D.az[i], az)));
+  if (sp.epi != EPI_FORCES && !(fl & FLAG_FIXEDPOS)) {
+    if (MIXED) {
+      vx = fma(sp.half_dt, D.ax[i] + ax, vx);
+      vy = fma(sp.half_dt, D.ay[i] + ay, vy);
+      vz = fma(sp.half_dt, D.az[i] + az, vz);
+    } else {
+      vx = dadd(vx, dmul(sp.half_dt, dadd(D.ax[i], ax)));
+      vy = dadd(vy, dmul(sp.half_dt, dadd(D.ay[i], ay)));
+      vz = dadd(vz, dmul(sp.half_dt, dadd(D.az[i], az)));
+    }
     D.vx[i] = vx;
     D.vy[i] = vy;
     D.vz[i] = vz;
@@ -88,11 +106,13 @@ __device__ __forceinline__ void finish_atom(const Dev& D, long long i, double Fx
   // KineticEnergy/Momentum skip tagged atoms (liblpmd/lpmd/properties.h:22-37,64-81)
   if (sp.kinetic && !(fl & (FLAG_FIXEDVEL | FLAG_FIXEDPOS))) {
     const double m = D.mass[i];
-    ke = dmul(dmul(0.5, m), ref_sq(vx, vy, vz));
+    ke = MIXED ? (0.5 * m) * fma(vx, vx, fma(vy, vy, vz * vz)) : dmul(dmul(0.5, m), ref_sq(vx, vy, vz));
     px = dmul(vx, m);
     py = dmul(vy, m);
     pz = dmul(vz, m);
   }
+  if (sp.epi == EPI_KICK_DRIFT) return drift_atom<MIXED>(D, S, i, sp.dt, vx, vy, vz, ax, ay, az);
+  return 0.0f;
 }
 
 // Writes the tile's FP64 partials (slots [lo, hi) of the 16) with overwrite or accumulate.
@@ -149,6 +169,7 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
     });
   }
   double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+  float d2 = 0.0f;
   if (active) {
     long long N = D.N;
     if (!sp.first) {
@@ -157,13 +178,14 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
       fz += D.dacc[2 * N + i];
     }
     if (sp.last) {
-      finish_atom(D, i, fx, fy, fz, sp, ke, px, py, pz);
+      d2 = finish_atom<0>(D, S, i, fx, fy, fz, sp, ke, px, py, pz);
     } else {
       D.dacc[i] = fx;
       D.dacc[N + i] = fy;
       D.dacc[2 * N + i] = fz;
     }
   }
+  track_displacement_warp(D, s, d2);
   // the full list counts each pair twice: halve energy, virial and stress
   double v[13] = {0.5 * ep, 0.5 * vir, 0.5 * sxx, 0.5 * sxy, 0.5 * sxz, 0.5 * sxy, 0.5 * syy,
                   0.5 * syz, 0.5 * sxz, 0.5 * syz, 0.5 * szz, ke, 0.0};
@@ -196,61 +218,84 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
 // guard band around rc^2 so the set of interacting pairs is the FP64 reference's.
 // ------------------------------------------------------------------------------------------
 
-template <int PC>
-__global__ void __launch_bounds__(TILE) k_force32(Dev D, PotParams P, StepParams sp) {
+template <int PC, int SPECIES>
+__global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepParams sp) {
   __shared__ float4 shifts[125];
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   load_shifts(S, shifts);
-  const long long i = D.tile_first[tile] + threadIdx.x;
+  const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;  // index within the system
+  const long long i = S.atom_base + li;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
-  long long qx = 0, qy = 0, qz = 0;
-  float ep = 0.f, vir = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  const float4* __restrict__ g32 = D.g32 + S.atom_base;
+  Fix fqx, fqy, fqz;
+  // sab = sum over pairs of f_a * r_b with f = g * r; stress_ab = -sab/2, virial = -trace/2
+  float ep = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
   const float rc2_lo = P.f[12], rc2_hi = P.f[13];
-  const float fscale = (float)FIX_F;
-  unsigned long long rechecks = 0;
+  unsigned rechecks = 0;
+  bool bad = false;
   if (active) {
-    const float4 gi = D.g32[i];
+    const float4 gi = g32[li];
     const int ti = __float_as_int(gi.w);
     const float phi_i = (PC == PC_EAM) ? D.phif[i] : 0.f;
-    for_each_candidate<NB_LIST>(D, S, i, [&](long long j, unsigned code) {
-      const float4 gj = D.g32[j];
-      const float4 sh = shifts[code];
-      float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-      float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 < rc2_hi) {
-        bool in = r2 < rc2_lo;
-        if (!in) {
-          in = exact_inside(D, S, i, j, P.rc2);
-          ++rechecks;
-        }
-        if (in && applies_to(P.spc_sum, ti, __float_as_int(gj.w))) {
-          float g, e;
-          if (PC == PC_PAIR) {
-            lj_pair32(P, __frcp_rn(r2), g, e);
-          } else {
-            eam_pair32(P, r2, phi_i, D.phif[j], g, e);
-          }
-          float gs = g * fscale;
-          qx += __float2ll_rn(gs * dx);
-          qy += __float2ll_rn(gs * dy);
-          qz += __float2ll_rn(gs * dz);
-          ep += e;
-          vir -= g * r2;
-          sxx -= g * dx * dx;
-          sxy -= g * dx * dy;
-          sxz -= g * dx * dz;
-          syy -= g * dy * dy;
-          syz -= g * dy * dz;
-          szz -= g * dz * dz;
-        }
+    const uint4* __restrict__ L = list_group(D, S, li, 0);
+    const int na = S.natoms;
+    const int cnt = D.ncount[i];
+    const int ng = (cnt + 3) >> 2;
+    // Branch-free body: every candidate is evaluated and out-of-range pairs are masked to
+    // zero, so lanes never diverge on the cutoff test (70% of Verlet-list entries are inside).
+    auto pair = [&](unsigned e, bool valid) {
+      const int j = (int)(e & LOCAL_MASK);
+      const float4 gj = g32[j];
+      const float4 sh = shifts[e >> CODE_SHIFT];
+      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      bool in = valid && r2 < rc2_lo;
+      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // inside the guard band: decide in FP64 like the reference
+        in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
+        ++rechecks;
       }
-    });
+      if (SPECIES) in = in && applies_to(P.spc_sum, ti, __float_as_int(gj.w));
+      float g, en;
+      if (PC == PC_PAIR) {
+        lj_pair32(P, rcp_approx(r2), g, en);
+      } else {
+        eam_pair32(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
+      }
+      g = in ? g : 0.0f;
+      en = in ? en : 0.0f;
+      const float fx = g * dx, fy = g * dy, fz = g * dz;
+      fqx.add_scaled32(fx);
+      fqy.add_scaled32(fy);
+      fqz.add_scaled32(fz);
+      ep += en;
+      sxx = fmaf(fx, dx, sxx);
+      sxy = fmaf(fx, dy, sxy);
+      sxz = fmaf(fx, dz, sxz);
+      syy = fmaf(fy, dy, syy);
+      syz = fmaf(fy, dz, syz);
+      szz = fmaf(fz, dz, szz);
+      bad |= fabsf(g * r2) > 4000.0f;  // |f| < 4096 eV/A keeps the fixed-point split exact
+    };
+    // Groups of four entries per 16-byte load; the next group is loaded before the current
+    // one is evaluated, so the list load of one group overlaps the gathers of the previous.
+    uint4 nxt = ng > 0 ? __ldg(L) : make_uint4(0u, 0u, 0u, 0u);
+    for (int q = 0; q < ng; ++q) {
+      const uint4 cur = nxt;
+      if (q + 1 < ng) nxt = __ldg(L + (long long)(q + 1) * na);
+      const int rem = cnt - 4 * q;
+      pair(cur.x, true);
+      pair(cur.y, rem > 1);
+      pair(cur.z, rem > 2);
+      pair(cur.w, rem > 3);
+    }
   }
   double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+  float d2 = 0.0f;
   if (active) {
     const long long N = D.N;
+    long long qx = fqx.value(), qy = fqy.value(), qz = fqz.value();
     if (!sp.first) {
       qx += D.facc[i];
       qy += D.facc[N + i];
@@ -258,36 +303,39 @@ __global__ void __launch_bounds__(TILE) k_force32(Dev D, PotParams P, StepParams
     }
     if (sp.last) {
       const double inv = 1.0 / FIX_F;
-      finish_atom(D, i, (double)qx * inv, (double)qy * inv, (double)qz * inv, sp, ke, px, py, pz);
+      d2 = finish_atom<1>(D, S, i, (double)qx * inv, (double)qy * inv, (double)qz * inv, sp, ke, px, py, pz);
     } else {
       D.facc[i] = qx;
       D.facc[N + i] = qy;
       D.facc[2 * N + i] = qz;
     }
-    if (rechecks) atomicAdd(&D.sst[s].rechecks, rechecks);
+    if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
+    if (bad) atomicOr(&D.sst[s].error, ERR_FIXED);
   }
-  // per-atom energy/virial/stress (halved: full list) to int64 fixed point, exact block sums
+  track_displacement_warp(D, s, d2);
+  // per-atom energy and stress (halved: full list) to int64 fixed point; exact block sums and
+  // one integer atomic per quantity into the system's accumulators
   const float es = (float)(0.5 * FIX_E);
-  long long v[11] = {__float2ll_rn(ep * es), __float2ll_rn(vir * es), __float2ll_rn(sxx * es),
-                     __float2ll_rn(sxy * es), __float2ll_rn(sxz * es), __float2ll_rn(sxy * es),
-                     __float2ll_rn(syy * es), __float2ll_rn(syz * es), __float2ll_rn(sxz * es),
-                     __float2ll_rn(syz * es), __float2ll_rn(szz * es)};
+  const float ms = -es;
+  long long v[11] = {fix64(ep * es), fix64((sxx + syy + szz) * ms), fix64(sxx * ms), fix64(sxy * ms),
+                     fix64(sxz * ms), fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms),
+                     fix64(syz * ms), fix64(szz * ms)};
   long long tot[11];
   block_sum<long long, 11>(v, tot);
   if (threadIdx.x == 0) {
-    long long* t = D.tile_i + (long long)tile * PART_I;
-    for (int k = 0; k < 11; ++k) t[k] = sp.first ? tot[k] : t[k] + tot[k];
+    unsigned long long* acc = D.sys_acc + (long long)s * SA_LEN;
+    for (int k = 0; k < 11; ++k) atomicAdd(acc + k, (unsigned long long)tot[k]);
   }
   if (sp.last) {
+    // kinetic energy and momentum: FP64 block sums in a fixed order, then exact int64 sums
+    // across blocks (2^-40 units per block)
     double k4[4] = {ke, px, py, pz};
     double kt[4];
     block_sum<double, 4>(k4, kt);
     if (threadIdx.x == 0) {
-      double* t = D.tile_d + (long long)tile * PART_D;
-      t[PD_KE] = kt[0];
-      t[PD_PX] = kt[1];
-      t[PD_PX + 1] = kt[2];
-      t[PD_PX + 2] = kt[3];
+      unsigned long long* acc = D.sys_acc + (long long)s * SA_LEN;
+      atomicAdd(acc + SA_KE, (unsigned long long)__double2ll_rn(kt[0] * FIX_KE));
+      for (int k = 0; k < 3; ++k) atomicAdd(acc + SA_P + k, (unsigned long long)__double2ll_rn(kt[1 + k] * FIX_KE));
     }
   }
 }
@@ -309,7 +357,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int fi
   if (active) {
     double rho = 0.0;
     if (MIXED) {
-      long long q = 0;
+      Fix q;
       const float4 gi = D.g32[i];
       const float rc2_lo = P.f[12], rc2_hi = P.f[13];
       const float scale = (float)FIX_RHO;
@@ -321,10 +369,10 @@ __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int fi
         if (r2 < rc2_hi) {
           bool in = r2 < rc2_lo;
           if (!in) in = exact_inside(D, S, i, j, P.rc2);
-          if (in) q += __float2ll_rn(eam_rho32(P, r2) * scale);
+          if (in) q.add(eam_rho32(P, r2) * scale);
         }
       });
-      rho = (double)q * (1.0 / FIX_RHO);
+      rho = (double)q.value() * (1.0 / FIX_RHO);
     } else {
       const double4_32a pi = D.g64[i];
       for_each_candidate<NB>(D, S, i, [&](long long j, unsigned) {
@@ -342,12 +390,20 @@ __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int fi
     D.phi[i] = phi;
     D.phif[i] = (float)phi;
   }
-  double v[1] = {F};
-  double t[1];
-  block_sum<double, 1>(v, t);
-  if (threadIdx.x == 0) {
-    double* td = D.tile_d + (long long)tile * PART_D;
-    td[PD_EEMBED] = first ? t[0] : td[PD_EEMBED] + t[0];
+  if (MIXED) {
+    // FP64 embedding energies summed exactly as int64 fixed point (2^-32 eV per atom)
+    long long v[1] = {active ? __double2ll_rn(F * FIX_E) : 0ll};
+    long long t[1];
+    block_sum<long long, 1>(v, t);
+    if (threadIdx.x == 0) atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_EEMBED, (unsigned long long)t[0]);
+  } else {
+    double v[1] = {F};
+    double t[1];
+    block_sum<double, 1>(v, t);
+    if (threadIdx.x == 0) {
+      double* td = D.tile_d + (long long)tile * PART_D;
+      td[PD_EEMBED] = first ? t[0] : td[PD_EEMBED] + t[0];
+    }
   }
 }
 
@@ -360,37 +416,38 @@ __global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_ste
   const SysDev& S = D.sysd[s];
   SysState& st = D.sst[s];
   double v[PART_D];
-  long long q[PART_I];
   for (int k = 0; k < PART_D; ++k) v[k] = 0.0;
-  for (int k = 0; k < PART_I; ++k) q[k] = 0;
-  for (int t = threadIdx.x; t < S.ntiles; t += blockDim.x) {
-    const double* td = D.tile_d + (long long)(S.tile_base + t) * PART_D;
-    for (int k = 0; k < PART_D; ++k) v[k] += td[k];
-    if (mixed) {
-      const long long* ti = D.tile_i + (long long)(S.tile_base + t) * PART_I;
-      for (int k = 0; k < PART_I; ++k) q[k] += ti[k];
+  if (!mixed) {
+    for (int t = threadIdx.x; t < S.ntiles; t += blockDim.x) {
+      const double* td = D.tile_d + (long long)(S.tile_base + t) * PART_D;
+      for (int k = 0; k < PART_D; ++k) v[k] += td[k];
     }
   }
   double tot[PART_D];
-  long long qt[PART_I];
-  block_sum<double, PART_D>(v, tot);
-  block_sum<long long, PART_I>(q, qt);
+  if (!mixed) block_sum<double, PART_D>(v, tot);  // block-uniform branch
   if (threadIdx.x == 0) {
+    if (mixed)
+      for (int k = 0; k < PART_D; ++k) tot[k] = 0.0;
     double epair = tot[PD_EPAIR], vir = tot[PD_VIR];
     double stress[9];
     for (int k = 0; k < 9; ++k) stress[k] = tot[PD_STRESS + k];
     if (mixed) {
-      const double inv = 1.0 / FIX_E;
-      epair = (double)qt[PI_EPAIR] * inv;
-      vir = (double)qt[PI_VIR] * inv;
-      for (int k = 0; k < 9; ++k) stress[k] = (double)qt[PI_STRESS + k] * inv;
+      const long long* acc = (const long long*)D.sys_acc + (long long)s * SA_LEN;
+      const double inv = 1.0 / FIX_E, invk = 1.0 / FIX_KE;
+      epair = (double)acc[SA_EPAIR] * inv;
+      vir = (double)acc[SA_VIR] * inv;
+      for (int k = 0; k < 9; ++k) stress[k] = (double)acc[SA_STRESS + k] * inv;
+      tot[PD_EEMBED] = (double)acc[SA_EEMBED] * inv;
+      tot[PD_KE] = (double)acc[SA_KE] * invk;
+      for (int k = 0; k < 3; ++k) tot[PD_PX + k] = (double)acc[SA_P + k] * invk;
     }
     if (count_step) st.step += 1;
     const double KIN2EV = 103.64269, KB = 8.6173422E-05, PRESSF = 160217.65;
     double epot = epair + tot[PD_EEMBED];
     double kin = dmul(tot[PD_KE], KIN2EV);
-    double temp = (S.natoms == 0) ? 0.0 : ddiv(dmul(2.0 / 3.0, kin), dmul(KB, (double)S.nfree));
-    double vol = dmul(dmul(S.L[0], S.L[1]), S.L[2]);
+    (void)KB;
+    double temp = (S.natoms == 0) ? 0.0 : ddiv(dmul(2.0 / 3.0, kin), S.kbn);
+    const double vol = S.vol, pv = S.pv;  // volume and pressfactor/volume, computed on the host
     double r[THERMO_LEN];
     r[0] = (double)st.step;
     r[1] = epot;
@@ -402,9 +459,10 @@ __global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_ste
     r[7] = tot[PD_PX + 1];
     r[8] = tot[PD_PX + 2];
     r[9] = vol;
-    r[10] = dmul(dmul(ddiv(PRESSF, vol), 1.0 / 3.0), vir);
-    r[11] = dmul(dmul(ddiv(PRESSF, vol), 2.0 / 3.0), kin);
-    r[12] = dmul(ddiv(PRESSF, vol), dadd(dmul(2.0 / 3.0, kin), dmul(1.0 / 3.0, vir)));
+    (void)PRESSF;
+    r[10] = dmul(dmul(pv, 1.0 / 3.0), vir);
+    r[11] = dmul(dmul(pv, 2.0 / 3.0), kin);
+    r[12] = dmul(pv, dadd(dmul(2.0 / 3.0, kin), dmul(1.0 / 3.0, vir)));
     for (int k = 0; k < 9; ++k) r[13 + k] = stress[k];
     double* last = D.thermo_last + (long long)s * THERMO_LEN;
     double* log = D.thermo_log + ((long long)s * D.log_cap + (st.step % D.log_cap)) * THERMO_LEN;

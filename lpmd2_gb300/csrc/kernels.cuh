@@ -27,7 +27,7 @@
 
 namespace gbmd {
 
-enum EpiMode { EPI_FORCES = 0, EPI_KICK = 1 };
+enum EpiMode { EPI_FORCES = 0, EPI_KICK = 1, EPI_KICK_DRIFT = 2 };
 
 struct StepParams {
   double dt;
@@ -65,6 +65,7 @@ __global__ void k_decide(Dev D, int nsys, int ucall_inc, int force_all, unsigned
     }
     st.ucalls += ucall_inc;
     if (S.mode == NB_ALLPAIRS) need = 0;
+    for (int k = 0; k < SA_LEN; ++k) D.sys_acc[(long long)s * SA_LEN + k] = 0ull;
     st.need_rebuild = need;
     st.force_rebuild = 0;
     if (need) {
@@ -88,9 +89,18 @@ __global__ void k_bin(Dev D) {
   if (!D.sst[s].need_rebuild) return;
   const SysDev& S = D.sysd[s];
   bool ok = true;
-  int cx = ref_cell_coord(D.x[i], S.L[0], S.n[0], ok);
-  int cy = ref_cell_coord(D.y[i], S.L[1], S.n[1], ok);
-  int cz = ref_cell_coord(D.z[i], S.L[2], S.n[2], ok);
+  int cx, cy, cz;
+  if (S.mode == NB_LIST) {
+    // Verlet-list grid: cells are wider than the list radius by a margin, so the binning may
+    // round differently from LinkedCell's; one multiply instead of a division per axis
+    cx = list_cell_coord(D.x[i] * S.ninv[0], S.n[0], ok);
+    cy = list_cell_coord(D.y[i] * S.ninv[1], S.n[1], ok);
+    cz = list_cell_coord(D.z[i] * S.ninv[2], S.n[2], ok);
+  } else {
+    cx = ref_cell_coord(D.x[i], S.L[0], S.n[0], ok);
+    cy = ref_cell_coord(D.y[i], S.L[1], S.n[1], ok);
+    cz = ref_cell_coord(D.z[i], S.L[2], S.n[2], ok);
+  }
   if (!ok) {
     atomicOr(&D.sst[s].error, ERR_OUTSIDE);
     cx = cy = cz = 0;
@@ -154,15 +164,31 @@ __global__ void k_scatter(Dev D) {
   D.perm[p] = (int)i;
 }
 
-// One thread per cell (grid.y = system): insertion sort of the cell's slots by original index.
+// One warp per cell (grid.y = system): orders the cell's slots by original index, the order in
+// which LinkedCell's head/next lists visit them.  Up to 32 atoms: each lane ranks its atom by
+// counting smaller tags across the warp; larger cells fall back to an insertion sort by lane 0.
 __global__ void k_cellsort(Dev D) {
   const int s = blockIdx.y;
   if (!D.sst[s].need_rebuild) return;
   const SysDev& S = D.sysd[s];
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (c >= S.ncells) return;
-  int g = S.cell_base + c;
-  int b = D.cstart[g], n = D.ccnt[g];
+  const int lane = threadIdx.x & 31;
+  const int g = S.cell_base + c;
+  const int b = D.cstart[g], n = D.ccnt[g];
+  if (n <= 32) {
+    int v = lane < n ? D.perm[b + lane] : 0;
+    int tv = lane < n ? D.tag[v] : 0x7fffffff;
+    int rank = 0;
+    for (int k = 0; k < n; ++k) {
+      int tk = __shfl_sync(0xffffffffu, tv, k);
+      rank += (tk < tv) ? 1 : 0;
+    }
+    __syncwarp();
+    if (lane < n) D.perm[b + rank] = v;
+    return;
+  }
+  if (lane != 0) return;
   for (int k = 1; k < n; ++k) {
     int v = D.perm[b + k];
     int tv = D.tag[v];
@@ -201,26 +227,52 @@ __global__ void k_permute(Dev D) {
   if (D.has_flags) D.sflags[p] = D.flags[o];
 }
 
-// Offset of x from the centre of cell coordinate c (edge d), wrapped into [-L/2, L/2).
+// Offset of x from the centre of cell coordinate c (edge d), wrapped into [-L/2, L/2).  Four
+// FP64-pipe operations on the common path (the FP64 unit is GB300's scarcest); the wrap is
+// only taken for atoms far from their home cell (outside the box in the input).
 __device__ __forceinline__ float home_offset(double x, int c, double d, double L, double Lh) {
-  double o = dsub(x, dmul(dadd((double)c, 0.5), d));
-  if (o >= Lh) o = dsub(o, L);
-  if (o < -Lh) o = dadd(o, L);
-  return (float)o;
+  double o = x - fma((double)c, d, 0.5 * d);
+  float of = (float)o;
+  if (fabsf(of) >= 0.999f * (float)Lh) {
+    if (o >= Lh) o = dsub(o, L);
+    if (o < -Lh) o = dadd(o, L);
+    of = (float)o;
+  }
+  return of;
 }
 
-__device__ __forceinline__ void refresh_gather(const Dev& D, const SysDev& S, long long p, bool set_ref) {
-  double xx = D.x[p], yy = D.y[p], zz = D.z[p];
-  int t = D.type[p];
-  D.g64[p] = make_double4_32a(xx, yy, zz, (double)t);
+// Gather copies of atom p at position (xx, yy, zz): the FP64 double4 and, for Verlet lists,
+// the FP32 offset from the home-cell centre (returned, for displacement tracking).
+__device__ __forceinline__ float4 write_gather(const Dev& D, const SysDev& S, long long p, double xx, double yy,
+                                               double zz, int t, double4_32a* g64, float4* g32) {
+  g64[p] = make_double4_32a(xx, yy, zz, (double)t);
+  float4 g = make_float4(0.f, 0.f, 0.f, __int_as_float(t));
   if (S.mode == NB_LIST) {
     int h = D.home[p] - S.cell_base;
     int cx = h % S.n[0], cy = (h / S.n[0]) % S.n[1], cz = h / (S.n[0] * S.n[1]);
-    float4 g = make_float4(home_offset(xx, cx, S.d[0], S.L[0], S.Lh[0]), home_offset(yy, cy, S.d[1], S.L[1], S.Lh[1]),
-                           home_offset(zz, cz, S.d[2], S.L[2], S.Lh[2]), __int_as_float(t));
-    D.g32[p] = g;
-    if (set_ref) D.ref[p] = g;
+    g = make_float4(home_offset(xx, cx, S.d[0], S.L[0], S.Lh[0]), home_offset(yy, cy, S.d[1], S.L[1], S.Lh[1]),
+                    home_offset(zz, cz, S.d[2], S.L[2], S.Lh[2]), __int_as_float(t));
+    g32[p] = g;
   }
+  return g;
+}
+
+__device__ __forceinline__ void refresh_gather(const Dev& D, const SysDev& S, long long p, bool set_ref) {
+  float4 g = write_gather(D, S, p, D.x[p], D.y[p], D.z[p], D.type[p], D.g64, D.g32);
+  if (set_ref && S.mode == NB_LIST) D.ref[p] = g;
+}
+
+// Squared displacement since the last list build (FP32 offsets, home cell unchanged).
+__device__ __forceinline__ float displacement2(const Dev& D, long long p, float4 g) {
+  float4 r = D.ref[p];
+  float dx = g.x - r.x, dy = g.y - r.y, dz = g.z - r.z;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// Largest displacement^2 of a warp whose lanes all belong to system s (whole tiles/blocks).
+__device__ __forceinline__ void track_displacement_warp(const Dev& D, int s, float d2) {
+  unsigned m = __reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(d2));
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(&D.sst[s].maxdisp2, m);
 }
 
 __global__ void k_copyback(Dev D) {
@@ -255,81 +307,123 @@ __global__ void k_copyback(Dev D) {
 
 __device__ __forceinline__ int shift_code(int kx, int ky, int kz) { return (kx + 2) + 5 * ((ky + 2) + 5 * (kz + 2)); }
 
-__global__ void k_buildlist(Dev D) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= D.N) return;
-  int s = D.sysid[i];
+// One warp per home cell (grid.y = system): the lanes hold up to 32 atoms of the cell, and the
+// atoms of each stencil cell are staged through shared memory 32 at a time; every lane then
+// tests the staged candidate against its own atom (broadcast reads, no divergence between
+// lanes, since all atoms of a cell share the stencil and its cell-shift codes).
+constexpr int LIST_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * LIST_WARPS) k_buildlist(Dev D) {
+  __shared__ float4 stage[LIST_WARPS][32];
+  const int s = blockIdx.y;
   if (!D.sst[s].need_rebuild) return;
   const SysDev& S = D.sysd[s];
   if (S.mode != NB_LIST) return;
-  const float4 gi = D.g32[i];
-  const int h = D.home[i] - S.cell_base;
-  const int cx = h % S.n[0], cy = (h / S.n[0]) % S.n[1], cz = h / (S.n[0] * S.n[1]);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * LIST_WARPS + w;
+  if (c >= S.ncells) return;
+  const int g0 = S.cell_base + c;
+  const int b0 = D.cstart[g0], n0 = D.ccnt[g0];
+  const int cx = c % S.n[0], cy = (c / S.n[0]) % S.n[1], cz = c / (S.n[0] * S.n[1]);
   const int R = S.stencil_r;
-  const long long li = i - S.atom_base;
-  unsigned* out = D.nl + S.nl_base + li;
   const int na = S.natoms;
-  int cnt = 0;
-  for (int dz = -R; dz <= R; ++dz) {
-    int zc = wrap_around(cz + dz, S.n[2]);
-    float sz = (float)dz * S.df[2];
-    for (int dy = -R; dy <= R; ++dy) {
-      int yc = wrap_around(cy + dy, S.n[1]);
-      float sy = (float)dy * S.df[1];
-      for (int dx = -R; dx <= R; ++dx) {
-        int xc = wrap_around(cx + dx, S.n[0]);
-        float sx = (float)dx * S.df[0];
-        int g = S.cell_base + (zc * S.n[1] + yc) * S.n[0] + xc;
-        int b = D.cstart[g], e = b + D.ccnt[g];
-        unsigned code = (unsigned)shift_code(dx, dy, dz) << CODE_SHIFT;
-        for (int j = b; j < e; ++j) {
-          if (j == i) continue;
-          float4 gj = D.g32[j];
-          float rx = (sx + gj.x) - gi.x, ry = (sy + gj.y) - gi.y, rz = (sz + gj.z) - gi.z;
-          float r2 = rx * rx + ry * ry + rz * rz;
-          if (r2 < S.rlist2f) {
-            if (cnt < D.maxnb) out[(long long)cnt * na] = code | (unsigned)(j - S.atom_base);
-            ++cnt;
+  float4* st = stage[w];
+  const int maxnb = D.maxnb;
+  for (int base = 0; base < n0; base += 32) {
+    const bool has = base + lane < n0;
+    const long long i = (long long)b0 + base + lane;
+    const int li = (int)(i - S.atom_base);
+    const float4 gi = has ? D.g32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rl2 = has ? S.rlist2f : -1.0f;  // lanes without an atom never match
+    unsigned* out = D.nl + S.nl_base + (long long)li * 4;
+    const long long gstride = (long long)na * 4;  // words between consecutive groups of four
+    int cnt = 0;
+    for (int dz = -R; dz <= R; ++dz) {
+      const int zc = wrap_around(cz + dz, S.n[2]);
+      const float sz = (float)dz * S.df[2];
+      for (int dy = -R; dy <= R; ++dy) {
+        const int yc = wrap_around(cy + dy, S.n[1]);
+        const float sy = (float)dy * S.df[1];
+        for (int dx = -R; dx <= R; ++dx) {
+          const int xc = wrap_around(cx + dx, S.n[0]);
+          const float sx = (float)dx * S.df[0];
+          const int g = S.cell_base + (zc * S.n[1] + yc) * S.n[0] + xc;
+          const int b = D.cstart[g], n = D.ccnt[g];
+          const unsigned code = (unsigned)shift_code(dx, dy, dz) << CODE_SHIFT;
+          const float ox = sx - gi.x, oy = sy - gi.y, oz = sz - gi.z;
+          for (int jb = 0; jb < n; jb += 32) {
+            __syncwarp();
+            if (jb + lane < n) st[lane] = D.g32[b + jb + lane];
+            __syncwarp();
+            const int m = min(32, n - jb);
+            const int jl0 = b + jb - (int)S.atom_base;
+            for (int k = 0; k < m; ++k) {
+              const float4 gj = st[k];
+              const float rx = ox + gj.x, ry = oy + gj.y, rz = oz + gj.z;
+              const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+              const int jl = jl0 + k;
+              if (r2 < rl2 && jl != li) {
+                if (cnt < maxnb) out[(cnt >> 2) * gstride + (cnt & 3)] = code | (unsigned)jl;
+                ++cnt;
+              }
+            }
           }
         }
       }
     }
+    if (has) {
+      D.ncount[i] = cnt < maxnb ? cnt : maxnb;
+      atomicMax(&D.sst[s].max_count, cnt);
+      if (cnt > maxnb) atomicOr(&D.sst[s].error, ERR_LIST);
+    }
   }
-  D.ncount[i] = cnt < D.maxnb ? cnt : D.maxnb;
-  atomicMax(&D.sst[s].max_count, cnt);
-  if (cnt > D.maxnb) atomicOr(&D.sst[s].error, ERR_LIST);
 }
 
 // ---------------------------------------------------------------------------------------------
 // Integration: drift half of velocity Verlet
 // ---------------------------------------------------------------------------------------------
 
-__global__ void k_drift(Dev D, double dt) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= D.N) return;
-  int s = D.sysid[i];
+// VelocityVerlet::AdvancePosition of atom i from the evaluation buffer into the output buffer:
+// newpos = x + v*dt + 0.5*a*dt*dt, then FittedInside.  The FP64 path rounds every product and
+// sum separately as the reference does; the mixed path uses two FP64 fused multiply-adds per
+// coordinate.  Returns the squared displacement since the last list build.
+template <int MIXED>
+__device__ __forceinline__ float drift_atom(const Dev& D, const SysDev& S, long long i, double dt, double vx,
+                                            double vy, double vz, double ax, double ay, double az) {
+  double nx = D.x[i], ny = D.y[i], nz = D.z[i];
+  if (!(D.has_flags && (D.flags[i] & FLAG_FIXEDPOS))) {
+    if (MIXED) {
+      const double h2 = 0.5 * dt * dt;
+      nx = fma(h2, ax, fma(dt, vx, nx));
+      ny = fma(h2, ay, fma(dt, vy, ny));
+      nz = fma(h2, az, fma(dt, vz, nz));
+    } else {
+      nx = dadd(dadd(nx, dmul(vx, dt)), dmul(dmul(dmul(0.5, ax), dt), dt));
+      ny = dadd(dadd(ny, dmul(vy, dt)), dmul(dmul(dmul(0.5, ay), dt), dt));
+      nz = dadd(dadd(nz, dmul(vz, dt)), dmul(dmul(dmul(0.5, az), dt), dt));
+    }
+    nx = ref_fitted(nx, S.L[0]);
+    ny = ref_fitted(ny, S.L[1]);
+    nz = ref_fitted(nz, S.L[2]);
+  }
+  D.xo[i] = nx;
+  D.yo[i] = ny;
+  D.zo[i] = nz;
+  float4 g = write_gather(D, S, i, nx, ny, nz, D.type[i], D.g64o, D.g32o);
+  return S.mode == NB_LIST ? displacement2(D, i, g) : 0.0f;
+}
+
+// Stand-alone drift (the first step of a run, before any fused force/drift launch).
+template <int MIXED>
+__global__ void __launch_bounds__(TILE) k_drift(Dev D, double dt) {
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
-  bool fixed = D.has_flags && (D.flags[i] & FLAG_FIXEDPOS);
-  if (!fixed) {
-    // newpos = x + v*dt + 0.5*a*dt*dt, then FittedInside
-    double nx = dadd(dadd(D.x[i], dmul(D.vx[i], dt)), dmul(dmul(dmul(0.5, D.ax[i]), dt), dt));
-    double ny = dadd(dadd(D.y[i], dmul(D.vy[i], dt)), dmul(dmul(dmul(0.5, D.ay[i]), dt), dt));
-    double nz = dadd(dadd(D.z[i], dmul(D.vz[i], dt)), dmul(dmul(dmul(0.5, D.az[i]), dt), dt));
-    D.x[i] = ref_fitted(nx, S.L[0]);
-    D.y[i] = ref_fitted(ny, S.L[1]);
-    D.z[i] = ref_fitted(nz, S.L[2]);
-  }
-  refresh_gather(D, S, i, false);
-  if (S.mode == NB_LIST) {
-    float4 g = D.g32[i], r = D.ref[i];
-    float dx = g.x - r.x, dy = g.y - r.y, dz = g.z - r.z;
-    float d2 = dx * dx + dy * dy + dz * dz;
-    unsigned bits = (unsigned)__float_as_int(d2);
-    // aggregate the maximum over the lanes of the same system before the global atomic
-    unsigned same = __match_any_sync(__activemask(), s);
-    unsigned m = __reduce_max_sync(same, bits);
-    if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicMax(&D.sst[s].maxdisp2, m);
-  }
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  float d2 = 0.0f;
+  if ((int)threadIdx.x < D.tile_count[tile])
+    d2 = drift_atom<MIXED>(D, S, i, dt, D.vx[i], D.vy[i], D.vz[i], D.ax[i], D.ay[i], D.az[i]);
+  track_displacement_warp(D, s, d2);
 }
 
 }  // namespace gbmd

@@ -40,6 +40,8 @@ constexpr int ERR_OUTSIDE = 1;     // atom far outside the box / NaN position
 constexpr int ERR_LIST = 2;        // neighbour list capacity exceeded
 constexpr int ERR_FIXED = 4;       // fixed-point range exceeded
 constexpr int ERR_CELL = 8;        // cell occupancy beyond the sort capacity
+constexpr int ERR_WAIT = 16;       // a bounded wait on an asynchronous copy gave up
+constexpr int RING = 4;            // shared-memory stages of the list ring in the force kernel
 
 // Per-tile partial-sum slots (FP64)
 enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX = 13 };
@@ -47,7 +49,7 @@ enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX
 enum { PI_EPAIR = 0, PI_VIR = 1, PI_STRESS = 2 };
 // Per-system int64 fixed-point accumulators of the mixed path (atomics from every block)
 enum { SA_EPAIR = 0, SA_VIR = 1, SA_STRESS = 2, SA_KE = 11, SA_P = 12, SA_EEMBED = 15, SA_LEN = 16 };
-constexpr double FIX_KE = 1099511627776.0;  // 2^40: kinetic energy (amu A^2/fs^2) and momentum
+constexpr double FIX_KE = 17592186044416.0;  // 2^44: kinetic energy (amu A^2/fs^2) and momentum
 
 struct SysDev {
   long long atom_base;
@@ -187,6 +189,56 @@ __device__ __forceinline__ int ref_cell_coord(double x, double L, int n, bool& o
     return 0;
   }
   return wrap_around((int)t, n);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bulk asynchronous copies (TMA engine, non-tensor form) with mbarrier completion.
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Orders shared-memory reads made through ordinary loads (by this thread, or by threads that a
+// preceding barrier synchronised with it) before this thread's next bulk copy into that memory.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for phase `phase` of the barrier with a bounded number of polls (each poll may suspend
+// the thread for a hardware-defined interval).  Returns false if the bound was hit.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
 }
 
 __device__ __forceinline__ int list_cell_coord(double t, int n, bool& ok) {

@@ -79,7 +79,9 @@ template <int MIXED>
 __device__ __forceinline__ float finish_atom(const Dev& D, const SysDev& S, long long i, double Fx, double Fy,
                                              double Fz, const StepParams& sp, double& ke, double& px, double& py,
                                              double& pz) {
-  const double fm = D.fm[i];
+  // mixed: F arrives in 2^-32 eV/A units; scaling fm by the power of two is exact and gives
+  // the same products as scaling F
+  const double fm = MIXED ? D.fm[i] * (1.0 / FIX_F) : D.fm[i];
   double ax = dmul(Fx, fm), ay = dmul(Fy, fm), az = dmul(Fz, fm);
   unsigned char fl = D.has_flags ? D.flags[i] : 0;
   if (fl & FLAG_FIXEDVEL) ax = ay = az = 0.0;
@@ -218,8 +220,13 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
 // guard band around rc^2 so the set of interacting pairs is the FP64 reference's.
 // ------------------------------------------------------------------------------------------
 
+// Resident blocks per SM the register allocation of the mixed force kernel is sized for.
+#ifndef GBMD_FORCE_MIN_BLOCKS
+#define GBMD_FORCE_MIN_BLOCKS 8
+#endif
+
 template <int PC, int SPECIES>
-__global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepParams sp) {
+__global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
   __shared__ float4 shifts[125];
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
@@ -235,21 +242,31 @@ __global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepPar
   const float rc2_lo = P.f[12], rc2_hi = P.f[13];
   unsigned rechecks = 0;
   bool bad = false;
-  if (active) {
-    const float4 gi = g32[li];
+  // Each warp streams its 32 atoms' list groups (32 x 16 bytes, contiguous for a fixed group
+  // index) through its own ring of shared-memory stages, filled by bulk asynchronous copies
+  // (TMA engine) that run RING groups ahead of the force evaluation.  Warps never wait on
+  // each other inside the loop.
+  __shared__ __align__(16) uint4 ring[TILE / 32][RING][32];
+  __shared__ __align__(8) unsigned long long bar[TILE / 32][RING];
+  {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = __float_as_int(gi.w);
-    const float phi_i = (PC == PC_EAM) ? D.phif[i] : 0.f;
-    const uint4* __restrict__ L = list_group(D, S, li, 0);
+    const float phi_i = (PC == PC_EAM && active) ? D.phif[i] : 0.f;
     const int na = S.natoms;
-    const int cnt = D.ncount[i];
+    const int cnt = active ? D.ncount[i] : 0;
     const int ng = (cnt + 3) >> 2;
     // Branch-free body: every candidate is evaluated and out-of-range pairs are masked to
     // zero, so lanes never diverge on the cutoff test (70% of Verlet-list entries are inside).
-    auto pair = [&](unsigned e, bool valid) {
+    // Returns g with f = g * d; the caller sums a group's four forces in FP32 and adds the
+    // group sum to the int64 fixed-point accumulators.
+    auto pair = [&](unsigned e, bool valid, float& dx, float& dy, float& dz) -> float {
       const int j = (int)(e & LOCAL_MASK);
       const float4 gj = g32[j];
       const float4 sh = shifts[e >> CODE_SHIFT];
-      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      dx = (sh.x + gj.x) - gi.x;
+      dy = (sh.y + gj.y) - gi.y;
+      dz = (sh.z + gj.z) - gi.z;
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       bool in = valid && r2 < rc2_lo;
       if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // inside the guard band: decide in FP64 like the reference
@@ -264,32 +281,61 @@ __global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepPar
         eam_pair32(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
       }
       g = in ? g : 0.0f;
-      en = in ? en : 0.0f;
+      ep += in ? en : 0.0f;
       const float fx = g * dx, fy = g * dy, fz = g * dz;
-      fqx.add_scaled32(fx);
-      fqy.add_scaled32(fy);
-      fqz.add_scaled32(fz);
-      ep += en;
       sxx = fmaf(fx, dx, sxx);
       sxy = fmaf(fx, dy, sxy);
       sxz = fmaf(fx, dz, sxz);
       syy = fmaf(fy, dy, syy);
       syz = fmaf(fy, dz, syz);
       szz = fmaf(fz, dz, szz);
-      bad |= fabsf(g * r2) > 4000.0f;  // |f| < 4096 eV/A keeps the fixed-point split exact
+      return g;
     };
-    // Groups of four entries per 16-byte load; the next group is loaded before the current
-    // one is evaluated, so the list load of one group overlaps the gathers of the previous.
-    uint4 nxt = ng > 0 ? __ldg(L) : make_uint4(0u, 0u, 0u, 0u);
-    for (int q = 0; q < ng; ++q) {
-      const uint4 cur = nxt;
-      if (q + 1 < ng) nxt = __ldg(L + (long long)(q + 1) * na);
-      const int rem = cnt - 4 * q;
-      pair(cur.x, true);
-      pair(cur.y, rem > 1);
-      pair(cur.z, rem > 2);
-      pair(cur.w, rem > 3);
+    const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
+    const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
+    const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
+    const uint4* src0 = list_group(D, S, wfirst, 0);
+    const unsigned bytes = (unsigned)wcount * 16u;
+    unsigned long long* wbar = bar[w];
+    if (lane == 0 && ngw > 0) {
+      for (int r = 0; r < RING; ++r) mbar_init(&wbar[r], 1);
+      mbar_init_fence();
+      for (int r = 0; r < RING && r < ngw; ++r) {
+        mbar_expect_tx(&wbar[r], bytes);
+        bulk_g2s(ring[w][r], src0 + (long long)r * na, bytes, &wbar[r]);
+      }
     }
+    __syncwarp();
+    bool waited = true;
+    for (int q = 0; q < ngw; ++q) {
+      const int r = q & (RING - 1);
+      if (!mbar_wait_bounded(&wbar[r], (unsigned)((q / RING) & 1))) waited = false;
+      const uint4 cur = ring[w][r][lane];
+      __syncwarp();  // every lane has its entry: the stage can be refilled
+      if (lane == 0 && q + RING < ngw) {
+        fence_proxy_async_shared();
+        mbar_expect_tx(&wbar[r], bytes);
+        bulk_g2s(ring[w][r], src0 + (long long)(q + RING) * na, bytes, &wbar[r]);
+      }
+      if (q < ng) {
+        const int rem = cnt - 4 * q;
+        float ax, ay, az, bx, by, bz;
+        float g0 = pair(cur.x, true, ax, ay, az);
+        float g1 = pair(cur.y, rem > 1, bx, by, bz);
+        float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
+        g0 = pair(cur.z, rem > 2, ax, ay, az);
+        g1 = pair(cur.w, rem > 3, bx, by, bz);
+        gx = fmaf(g1, bx, fmaf(g0, ax, gx));
+        gy = fmaf(g1, by, fmaf(g0, ay, gy));
+        gz = fmaf(g1, bz, fmaf(g0, az, gz));
+        fqx.add_scaled32(gx);
+        fqy.add_scaled32(gy);
+        fqz.add_scaled32(gz);
+        // |group force| < 4096 eV/A keeps the fixed-point split exact
+        bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+      }
+    }
+    if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
   }
   double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
   float d2 = 0.0f;
@@ -302,8 +348,7 @@ __global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepPar
       qz += D.facc[2 * N + i];
     }
     if (sp.last) {
-      const double inv = 1.0 / FIX_F;
-      d2 = finish_atom<1>(D, S, i, (double)qx * inv, (double)qy * inv, (double)qz * inv, sp, ke, px, py, pz);
+      d2 = finish_atom<1>(D, S, i, (double)qx, (double)qy, (double)qz, sp, ke, px, py, pz);
     } else {
       D.facc[i] = qx;
       D.facc[N + i] = qy;
@@ -327,15 +372,17 @@ __global__ void __launch_bounds__(TILE, 6) k_force32(Dev D, PotParams P, StepPar
     for (int k = 0; k < 11; ++k) atomicAdd(acc + k, (unsigned long long)tot[k]);
   }
   if (sp.last) {
-    // kinetic energy and momentum: FP64 block sums in a fixed order, then exact int64 sums
-    // across blocks (2^-40 units per block)
-    double k4[4] = {ke, px, py, pz};
-    double kt[4];
-    block_sum<double, 4>(k4, kt);
+    // kinetic energy: FP64 warp sums in a fixed order, rounded once per warp to int64 (2^-44
+    // units); momentum: rounded per atom.  Exact int64 sums from there on.
+    const double kw = warp_sum(ke);
+    long long k4[4] = {(threadIdx.x & 31) == 0 ? __double2ll_rn(kw * FIX_KE) : 0ll, __double2ll_rn(px * FIX_KE),
+                       __double2ll_rn(py * FIX_KE), __double2ll_rn(pz * FIX_KE)};
+    long long kt[4];
+    block_sum<long long, 4>(k4, kt);
     if (threadIdx.x == 0) {
       unsigned long long* acc = D.sys_acc + (long long)s * SA_LEN;
-      atomicAdd(acc + SA_KE, (unsigned long long)__double2ll_rn(kt[0] * FIX_KE));
-      for (int k = 0; k < 3; ++k) atomicAdd(acc + SA_P + k, (unsigned long long)__double2ll_rn(kt[1 + k] * FIX_KE));
+      atomicAdd(acc + SA_KE, (unsigned long long)kt[0]);
+      for (int k = 0; k < 3; ++k) atomicAdd(acc + SA_P + k, (unsigned long long)kt[1 + k]);
     }
   }
 }

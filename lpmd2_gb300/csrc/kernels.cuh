@@ -357,15 +357,22 @@ __global__ void __launch_bounds__(32 * LIST_WARPS) k_buildlist(Dev D) {
             __syncwarp();
             const int m = min(32, n - jb);
             const int jl0 = b + jb - (int)S.atom_base;
+            // pass 1: a bit per staged candidate inside the list radius (branch-free)
+            unsigned hits = 0u;
             for (int k = 0; k < m; ++k) {
               const float4 gj = st[k];
               const float rx = ox + gj.x, ry = oy + gj.y, rz = oz + gj.z;
               const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-              const int jl = jl0 + k;
-              if (r2 < rl2 && jl != li) {
-                if (cnt < maxnb) out[(cnt >> 2) * gstride + (cnt & 3)] = code | (unsigned)jl;
-                ++cnt;
-              }
+              hits |= (r2 < rl2 ? 1u : 0u) << k;
+            }
+            const int self = li - jl0;  // drop the atom itself
+            if (self >= 0 && self < 32) hits &= ~(1u << self);
+            // pass 2: append the hits in candidate order
+            while (hits) {
+              const int k = __ffs(hits) - 1;
+              hits &= hits - 1u;
+              if (cnt < maxnb) out[(cnt >> 2) * gstride + (cnt & 3)] = code | (unsigned)(jl0 + k);
+              ++cnt;
             }
           }
         }

@@ -17,6 +17,7 @@ libgbmd.so has not been built.
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
 import numpy as np
@@ -120,11 +121,15 @@ _LIB = None
 
 
 def load(path: Path | str | None = None):
-    """Loads libgbmd.so (built by __graft_entry__.build() or ``make -C lpmd2_gb300/csrc``)."""
+    """Loads libgbmd.so (built by __graft_entry__.build() or ``make -C lpmd2_gb300/csrc``).
+
+    The environment variable GBMD_LIBRARY names another build of the library (for example a
+    variant compiled with different tuning flags) to load instead of the in-tree one.
+    """
     global _LIB
     if _LIB is not None and path is None:
         return _LIB
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("GBMD_LIBRARY", LIB_PATH))
     if not p.exists():
         raise ImportError(f"libgbmd.so not built ({p}); run __graft_entry__.build()")
     lib = ctypes.CDLL(str(p))

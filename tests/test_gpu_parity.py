@@ -96,7 +96,9 @@ def test_forces_at_thermalised_state(case, precision):
     assert rel_norm_err(acc, g["acc"]) <= tol_f
     assert abs(th[1] - ref[1]) <= tol_e * abs(ref[1])
     assert abs(th[5] - ref[5]) <= tol_w * abs(ref[5])
-    assert abs(th[2] - ref[2]) <= 1e-12 * abs(ref[2])  # kinetic energy is FP64 in both paths
+    # kinetic energy: FP64 per atom in both paths; the mixed path sums blocks as int64 fixed
+    # point (2^-44 amu A^2/fs^2 per block), hence the looser bound there
+    assert abs(th[2] - ref[2]) <= (1e-12 if precision == "fp64" else 1e-11) * abs(ref[2])
 
 
 @pytest.mark.parametrize("case", [c for c in GOLDEN_CASES if c != "kat108"])

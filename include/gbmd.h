@@ -225,6 +225,44 @@ gbmd_status gbmd_batch_thermo(gbmd_batch* batch, int sys, gbmd_thermo* out);
 gbmd_status gbmd_batch_stats(gbmd_batch* batch, gbmd_stats* out);
 gbmd_status gbmd_batch_stream(gbmd_batch* batch, void** stream);
 
+/* ---------------------------------------------------------------------------------------- */
+/* Pair forces without device allocation                                                    */
+/* ---------------------------------------------------------------------------------------- */
+
+/* Largest system gbmd_pair_forces_static accepts (atoms). */
+#define GBMD_STATIC_MAX_ATOMS 16384
+
+/* FP64 pair forces, energy, virial and stress of ONE periodic orthorhombic system whose
+ * positions are already in device memory, computed without allocating any device memory.
+ * No counterpart in the reference: it packages the minimum-image pair-force evaluation
+ * (PairPotential::UpdateForces over MinimumImageCellManager, liblpmd/simulation/
+ * pairpotential.cc:35-75, plugins/minimumimage.cc:68-100) for callers that cannot allocate
+ * at call time -- host code that hands the whole device memory budget to its own pool, or a
+ * latency-bound loop that must not pay for cudaMalloc/cudaFree -- and that bring their own
+ * device buffers.  The gbmd_sim_* path allocates its pools in gbmd_sim_create instead.
+ *
+ *   plugin  a "lennardjones" potential plugin; its cutoff applies, its species
+ *           restriction does not (every pair interacts, as with gbmd_sim_add_potential
+ *           and s1 = s2 = -1)
+ *   pos     device, 3*n doubles (x0 y0 z0 x1 ...), minimum-image displacements as the
+ *           reference's Displacement (one wrap of each component)
+ *   n       1..GBMD_STATIC_MAX_ATOMS; anything else is GBMD_ERR_INVALID with a message
+ *   box     host, 3 doubles: the cell's edge lengths
+ *   force   device, 3*n doubles, written: forces in eV/A (no forcefactor/mass scaling)
+ *   out     device, 11 doubles, written: pair energy (eV), virial, stress xx xy xz yx yy yz
+ *           zx zy zz -- the values gbmd_sim_thermo reports for the same system
+ *   stream  cudaStream_t the two kernels are queued on (NULL: the default stream); the call
+ *           returns without waiting for them
+ *
+ * Scratch: the per-block partial sums live in a fixed 11 KB device array inside the
+ * library, overwritten by every call; the caller's output buffers need not start at zero.
+ * The first call on a device (with that device current) looks the array up, which may load
+ * the module: make that first call before anything that must not see module loading, such
+ * as stream capture.  Calls that overlap in time on one device (other host threads, other
+ * streams) share the array and race: serialise them. */
+gbmd_status gbmd_pair_forces_static(const gbmd_plugin* plugin, const double* pos, int n, const double* box,
+                                    double* force, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -370,6 +370,17 @@ gbmd_status gbmd_potential_eval(const gbmd_plugin* p, int what, const double* ar
   return guarded([&] { potential_eval(p->spec.pot, what, args, out); });
 }
 
+gbmd_status gbmd_pair_forces_static(const gbmd_plugin* p, const double* pos, int n, const double* box, double* force,
+                                    double* out, void* stream) {
+  if (!p || !pos || !box || !force || !out) return fail(GBMD_ERR_INVALID, "null argument");
+  if (p->spec.kind != GBMD_KIND_POTENTIAL) return fail(GBMD_ERR_INVALID, "not a potential");
+  return guarded([&] {
+    PotParams P = p->spec.pot;
+    P.spc_sum = -2;  // every pair interacts
+    pair_forces_static(P, pos, n, box, force, out, stream);
+  });
+}
+
 // ---- simulation ----
 
 gbmd_status gbmd_sim_create(int device, int64_t natoms, const double cell[3], gbmd_sim** out) {

@@ -128,6 +128,10 @@ struct PluginSpec {
 
 PluginSpec make_plugin(const std::string& name, const std::string& args);
 void potential_eval(const PotParams& p, int what, const double* args, double* out);
+// Pair forces of one small system with no device allocation (static_forces.cu); stream is a
+// cudaStream_t.
+void pair_forces_static(const PotParams& P, const double* pos, int n, const double* box, double* force, double* out,
+                        void* stream);
 PotParams finalize_potential(int kind, const double* params, int s1, int s2);
 
 }  // namespace gbmd

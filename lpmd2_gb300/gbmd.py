@@ -115,6 +115,8 @@ _SIGS = {
     "gbmd_batch_thermo": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(Thermo)]),
     "gbmd_batch_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "gbmd_batch_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "gbmd_pair_forces_static": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 _LIB = None
@@ -176,6 +178,19 @@ def device_count() -> int:
     c = ctypes.c_int(0)
     _check(load().gbmd_device_count(ctypes.byref(c)))
     return c.value
+
+
+def pair_forces_static(plugin: "Plugin", pos_ptr: int, n: int, box, force_ptr: int, out_ptr: int,
+                       stream: int = 0) -> None:
+    """gbmd_pair_forces_static: pair forces of one small system from device pointers.
+
+    pos_ptr (3n doubles), force_ptr (3n doubles) and out_ptr (11 doubles) are device
+    addresses owned by the caller; nothing is allocated.  The work is queued on ``stream``.
+    """
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    if b.shape != (3,):
+        raise ValueError("box must hold 3 edge lengths")
+    _check(load().gbmd_pair_forces_static(plugin.h, pos_ptr, int(n), _p(b), force_ptr, out_ptr, stream or None))
 
 
 class Plugin:

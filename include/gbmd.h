@@ -212,6 +212,11 @@ void gbmd_batch_destroy(gbmd_batch* batch);
 gbmd_status gbmd_batch_set_atoms(gbmd_batch* batch, int sys, const double* pos, const double* vel,
                                  const int32_t* Z, const double* mass);
 gbmd_status gbmd_batch_get_atoms(gbmd_batch* batch, int sys, double* pos, double* vel, double* acc);
+/* Takes a system out of (active = 0) or back into (1) the work of later calls: every kernel
+ * skips an inactive system and its positions, velocities and counters stay as they were.
+ * Serving retires finished jobs this way while the rest of the batch runs on.  No
+ * counterpart in the reference (one LPMD process runs one system). */
+gbmd_status gbmd_batch_set_active(gbmd_batch* batch, int sys, int active);
 /* The same cell manager / potential / integrator plugins apply to every system. */
 gbmd_status gbmd_batch_set_cell_manager(gbmd_batch* batch, const gbmd_plugin* cellmanager);
 gbmd_status gbmd_batch_add_potential(gbmd_batch* batch, const gbmd_plugin* potential, int s1, int s2);

@@ -545,6 +545,10 @@ gbmd_status gbmd_batch_set_atoms(gbmd_batch* batch, int sys, const double* pos, 
   BATCH_GUARD(batch->eng->set_atoms(sys, pos, vel, nullptr, Z, mass));
 }
 
+gbmd_status gbmd_batch_set_active(gbmd_batch* batch, int sys, int active) {
+  BATCH_GUARD(batch->eng->set_active(sys, active != 0));
+}
+
 gbmd_status gbmd_batch_get_atoms(gbmd_batch* batch, int sys, double* pos, double* vel, double* acc) {
   BATCH_GUARD(batch->eng->get_atoms(sys, pos, vel, acc));
 }

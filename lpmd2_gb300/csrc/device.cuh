@@ -75,6 +75,7 @@ struct SysDev {
   double pv;            // pressfactor / volume
   double kbn;           // KBOLTZMANN * nfree
   double ninv[3];       // n / L: binning multiplier of the Verlet-list grid
+  int active;           // 0: every kernel skips the system (its state is left as it was)
 };
 
 struct SysState {

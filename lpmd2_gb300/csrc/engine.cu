@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 
 #include "forces.cuh"
@@ -13,6 +14,23 @@
 namespace gbmd {
 
 namespace {
+
+// Device allocations and frees may synchronise the device, which must not happen while
+// another thread's engine captures a CUDA graph; this process-wide lock keeps the two apart
+// (engines driven from several host threads, as the job server does).
+std::recursive_mutex g_dev_mu;
+
+template <class T>
+cudaError_t dev_malloc(T** p, size_t bytes) {
+  std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
+  return cudaMalloc((void**)p, bytes);
+}
+
+void dev_free(void* p) {
+  if (!p) return;
+  std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
+  cudaFree(p);
+}
 
 void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
@@ -312,7 +330,7 @@ struct Engine::Impl {
   T* alloc(size_t n, bool cellpool = false) {
     void* p = nullptr;
     size_t b = sizeof(T) * (n ? n : 1);
-    cudaError_t e = cudaMalloc(&p, b);
+    cudaError_t e = dev_malloc(&p, b);
     if (e != cudaSuccess) {
       cudaGetLastError();
       throw Error(6, "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e));
@@ -324,7 +342,7 @@ struct Engine::Impl {
   }
 
   void free_cells() {
-    for (void* p : cell_allocs) cudaFree(p);
+    for (void* p : cell_allocs) dev_free(p);
     cell_allocs.clear();
     cell_bytes = 0;
   }
@@ -402,6 +420,7 @@ struct Engine::Impl {
       S.pv = 160217.65 / S.vol;  // pressfactor / Cell().Volume() (simulationbuilder.cc:86,112)
       S.kbn = 8.6173422E-05 * (double)S.nfree;
       S.each = 1;
+      S.active = 1;
     }
     // per-atom arrays
     const size_t n = (size_t)N;
@@ -480,7 +499,7 @@ struct Engine::Impl {
       cudaEventDestroy(m.b);
     }
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
-    for (void* p : allocs) cudaFree(p);
+    for (void* p : allocs) dev_free(p);
     free_cells();
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
@@ -735,7 +754,8 @@ struct Engine::Impl {
     CK(cudaStreamSynchronize(stream));
     collect_marks();
     std::vector<SysState> hs(nsys);
-    CK(cudaMemcpy(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
     int err = 0, maxc = 0;
     long long rb = 0;
     unsigned long long rech = 0;
@@ -765,7 +785,8 @@ struct Engine::Impl {
       check_launch("rebuild");
       CK(cudaStreamSynchronize(stream));
       std::vector<SysState> hs(nsys);
-      CK(cudaMemcpy(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpyAsync(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
       int maxc = 0, err = 0;
       for (const auto& x : hs) {
         maxc = std::max(maxc, x.max_count);
@@ -777,7 +798,10 @@ struct Engine::Impl {
       // grow: re-allocate the list with room to spare and rebuild from scratch
       int maxnb = (int)std::ceil(maxc * 1.4) + 16;
       maxnb = (maxnb + 7) & ~7;
-      cudaFree(D.nl);
+      long long old_entries = 0;
+      for (const auto& S : sysd) old_entries += (long long)S.natoms * D.maxnb;
+      cell_bytes -= sizeof(unsigned) * (size_t)(old_entries ? old_entries : 1);
+      dev_free(D.nl);
       cell_allocs.erase(std::find(cell_allocs.begin(), cell_allocs.end(), (void*)D.nl));
       alloc_list(maxnb);
       upload_sysd();
@@ -835,6 +859,7 @@ struct Engine::Impl {
   }
 
   void build_graph(int nsteps) {
+    std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
     drop_graph();
     CK(cudaGraphCreate(&graph, 0));
     bool cond = graph_mode == 2;
@@ -968,6 +993,17 @@ Engine::Engine(int device, const std::vector<int64_t>& natoms, const std::vector
 
 Engine::~Engine() { delete d_; }
 
+void Engine::set_active(int sys, bool on) {
+  Impl& I = *d_;
+  if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
+  CK(cudaSetDevice(I.device));
+  // a system coming back has no pending drift: re-evaluate the batch's forces (identical
+  // values for the systems that kept running) and drift again before the next step
+  if (on && !I.sysd[sys].active) I.forces_valid = false;
+  I.sysd[sys].active = on ? 1 : 0;
+  I.upload_sysd();
+}
+
 void Engine::set_atoms(int sys, const double* pos, const double* vel, const double* acc, const int32_t* Z,
                        const double* mass) {
   Impl& I = *d_;
@@ -978,12 +1014,10 @@ void Engine::set_atoms(int sys, const double* pos, const double* vel, const doub
   const int n = (int)I.natoms[sys];
   if (n == 0) return;
   const size_t v3 = sizeof(double) * 3 * n;
-  // one staging buffer: pos | vel | acc | mass (doubles) then Z (ints)
-  size_t tot = 3 * v3 + sizeof(double) * n + sizeof(int) * n;
-  char* stg = nullptr;
-  CK(cudaMalloc(&stg, tot));
-  try {
-    double* dp = (double*)stg;
+  // staging in the permutation scratch (11 doubles per atom, idle outside a rebuild and
+  // ordered with it on the stream): pos | vel | acc | mass (doubles) then Z (ints)
+  {
+    double* dp = I.D.sdbl;
     double* dv = dp + 3 * n;
     double* da = dv + 3 * n;
     double* dm = da + 3 * n;
@@ -1000,11 +1034,7 @@ void Engine::set_atoms(int sys, const double* pos, const double* vel, const doub
     I.launched();
     I.check_launch("set_atoms");
     CK(cudaStreamSynchronize(I.stream));
-  } catch (...) {
-    cudaFree(stg);
-    throw;
   }
-  cudaFree(stg);
   I.forces_valid = false;
   I.forces_valid_layout = false;
 }
@@ -1022,12 +1052,12 @@ void Engine::set_flags(int sys, const uint8_t* flags) {
   I.sysd[sys].kbn = 8.6173422E-05 * (double)(n - nfixed);
   if (n == 0) return;
   unsigned char* df = nullptr;
-  CK(cudaMalloc(&df, n));
+  CK(dev_malloc(&df, n));
   if (flags) CK(cudaMemcpyAsync(df, flags, n, cudaMemcpyHostToDevice, I.stream));
   k_set_flags<<<nblocks(n, 256), 256, 0, I.stream>>>(I.D, I.atom_base[sys], n, flags ? df : nullptr);
   I.launched();
   CK(cudaStreamSynchronize(I.stream));
-  cudaFree(df);
+  dev_free(df);
   if (nfixed) I.flags_any = true;
   I.D.has_flags = I.flags_any ? 1 : 0;
   I.upload_sysd();
@@ -1042,16 +1072,13 @@ void Engine::get_atoms(int sys, double* pos, double* vel, double* acc) {
   const int n = (int)I.natoms[sys];
   if (n == 0) return;
   const size_t v3 = sizeof(double) * 3 * n;
-  double* stg = nullptr;
-  CK(cudaMalloc(&stg, 3 * v3));
+  double* stg = I.D.sdbl;  // staging in the permutation scratch (see set_atoms)
   k_get_atoms<<<nblocks(n, 256), 256, 0, I.stream>>>(I.D, I.atom_base[sys], n, stg, stg + 3 * n, stg + 6 * n);
   I.launched();
   if (pos) CK(cudaMemcpyAsync(pos, stg, v3, cudaMemcpyDeviceToHost, I.stream));
   if (vel) CK(cudaMemcpyAsync(vel, stg + 3 * n, v3, cudaMemcpyDeviceToHost, I.stream));
   if (acc) CK(cudaMemcpyAsync(acc, stg + 6 * n, v3, cudaMemcpyDeviceToHost, I.stream));
-  cudaError_t e = cudaStreamSynchronize(I.stream);
-  cudaFree(stg);
-  ck(e, "get_atoms");
+  ck(cudaStreamSynchronize(I.stream), "get_atoms");
 }
 
 void Engine::set_cell_manager(const CellManagerCfg& cfg) {
@@ -1141,10 +1168,11 @@ int64_t Engine::thermo_log(int sys, double* out, int64_t cap) {
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
   CK(cudaSetDevice(I.device));
   std::vector<double> all((size_t)I.log_cap * THERMO_LEN);
-  CK(cudaMemcpy(all.data(), I.D.thermo_log + (size_t)sys * I.log_cap * THERMO_LEN, sizeof(double) * all.size(),
-                cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(all.data(), I.D.thermo_log + (size_t)sys * I.log_cap * THERMO_LEN,
+                     sizeof(double) * all.size(), cudaMemcpyDeviceToHost, I.stream));
   SysState hs;
-  CK(cudaMemcpy(&hs, I.d_sst + sys, sizeof(SysState), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&hs, I.d_sst + sys, sizeof(SysState), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
   long long last = hs.step;
   long long first = std::max<long long>(1, last - I.log_cap + 1);
   if (!I.read_from.count(sys)) I.read_from[sys] = 1;
@@ -1185,8 +1213,8 @@ void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t*
   const float lo = (float)(rc2 * (1.0 - 8e-6)), hi = (float)(rc2 * (1.0 + 8e-6));
   const bool mixed = I.precision == PREC_MIXED;
   long long *dc = nullptr, *doff = nullptr, *didx = nullptr;
-  CK(cudaMalloc(&dc, sizeof(long long) * std::max(n, 1)));
-  CK(cudaMalloc(&doff, sizeof(long long) * std::max(n, 1)));
+  CK(dev_malloc(&dc, sizeof(long long) * std::max(n, 1)));
+  CK(dev_malloc(&doff, sizeof(long long) * std::max(n, 1)));
   auto launch = [&](long long* cnt, const long long* off, long long* ix) {
     const unsigned nb = nblocks(n, 128);
     if (n == 0) return;
@@ -1218,21 +1246,21 @@ void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t*
     if (total) *total = t;
     if (idx && t > 0) {
       if (cap < t) throw Error(9, "neighbour index buffer too small");
-      CK(cudaMalloc(&didx, sizeof(long long) * t));
+      CK(dev_malloc(&didx, sizeof(long long) * t));
       CK(cudaMemcpyAsync(doff, ho.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, I.stream));
       launch(nullptr, doff, didx);
       CK(cudaMemcpyAsync(idx, didx, sizeof(long long) * t, cudaMemcpyDeviceToHost, I.stream));
       CK(cudaStreamSynchronize(I.stream));
     }
   } catch (...) {
-    cudaFree(dc);
-    cudaFree(doff);
-    cudaFree(didx);
+    dev_free(dc);
+    dev_free(doff);
+    dev_free(didx);
     throw;
   }
-  cudaFree(dc);
-  cudaFree(doff);
-  cudaFree(didx);
+  dev_free(dc);
+  dev_free(doff);
+  dev_free(didx);
 }
 
 void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* order) {
@@ -1268,16 +1296,16 @@ void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* orde
   I.any_list = any_list;
   const int na = I.sysd[sys].natoms;
   long long *dc = nullptr, *dord = nullptr;
-  CK(cudaMalloc(&dc, sizeof(long long) * std::max(na, 1)));
-  CK(cudaMalloc(&dord, sizeof(long long) * std::max(na, 1)));
+  CK(dev_malloc(&dc, sizeof(long long) * std::max(na, 1)));
+  CK(dev_malloc(&dord, sizeof(long long) * std::max(na, 1)));
   if (na > 0) k_cells_out<<<nblocks(na, 128), 128, 0, I.stream>>>(I.D, sys, dc, dord);
   I.check_launch("cell_sort");
   std::vector<long long> hc(na), ho(na);
   CK(cudaMemcpyAsync(hc.data(), dc, sizeof(long long) * na, cudaMemcpyDeviceToHost, I.stream));
   CK(cudaMemcpyAsync(ho.data(), dord, sizeof(long long) * na, cudaMemcpyDeviceToHost, I.stream));
   CK(cudaStreamSynchronize(I.stream));
-  cudaFree(dc);
-  cudaFree(dord);
+  dev_free(dc);
+  dev_free(dord);
   for (int k = 0; k < na; ++k) {
     if (cell) cell[k] = hc[k];
     if (order) order[k] = ho[k];

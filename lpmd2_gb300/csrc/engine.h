@@ -88,6 +88,8 @@ class Engine {
                  const double* mass);
   void set_flags(int sys, const uint8_t* flags);
   void get_atoms(int sys, double* pos, double* vel, double* acc);
+  // Inactive systems are skipped by every kernel; their state is left as it was.
+  void set_active(int sys, bool on);
 
   void set_cell_manager(const CellManagerCfg& cfg);
   void add_potential(const PotParams& p);

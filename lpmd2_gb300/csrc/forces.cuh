@@ -132,6 +132,10 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
+  if (!S.active) {  // whole block: one tile belongs to one system
+    if (sp.epi == EPI_KICK_DRIFT && sp.last) hold_tile(D, S, tile, true);
+    return;
+  }
   const long long i = D.tile_first[tile] + threadIdx.x;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
   double fx = 0.0, fy = 0.0, fz = 0.0, ep = 0.0, vir = 0.0;
@@ -231,6 +235,10 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
+  if (!S.active) {  // whole block: one tile belongs to one system
+    if (sp.epi == EPI_KICK_DRIFT && sp.last) hold_tile(D, S, tile, true);
+    return;
+  }
   load_shifts(S, shifts);
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;  // index within the system
   const long long i = S.atom_base + li;
@@ -397,6 +405,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int fi
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
+  if (!S.active) return;  // whole block: one tile belongs to one system
   if (MIXED) load_shifts(S, shifts);
   const long long i = D.tile_first[tile] + threadIdx.x;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
@@ -462,6 +471,7 @@ __global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_ste
   const int s = blockIdx.x;
   const SysDev& S = D.sysd[s];
   SysState& st = D.sst[s];
+  if (!S.active) return;
   double v[PART_D];
   for (int k = 0; k < PART_D; ++k) v[k] = 0.0;
   if (!mixed) {

@@ -52,6 +52,10 @@ __global__ void k_decide(Dev D, int nsys, int ucall_inc, int force_all, unsigned
   for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
     const SysDev& S = D.sysd[s];
     SysState& st = D.sst[s];
+    if (!S.active) {
+      st.need_rebuild = 0;
+      continue;
+    }
     int need = force_all | st.force_rebuild;
     if (S.mode == NB_CELLS) need = 1;
     if (S.mode == NB_LIST) {
@@ -420,12 +424,39 @@ __device__ __forceinline__ float drift_atom(const Dev& D, const SysDev& S, long 
   return S.mode == NB_LIST ? displacement2(D, i, g) : 0.0f;
 }
 
+// Keeps an inactive system's committed positions in place across a launch that writes the
+// other position buffer.  A fused force+drift launch reads the pending buffer (x) and writes
+// the committed one (xo), after which the buffers swap roles: copy xo -> x (to_read = true).
+// A stand-alone drift reads the committed buffer (x) and writes the pending one (xo): copy
+// x -> xo (to_read = false).
+__device__ __forceinline__ void hold_tile(const Dev& D, const SysDev& S, int tile, bool to_read) {
+  if ((int)threadIdx.x >= D.tile_count[tile]) return;
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  if (to_read) {
+    D.x[i] = D.xo[i];
+    D.y[i] = D.yo[i];
+    D.z[i] = D.zo[i];
+    D.g64[i] = D.g64o[i];
+    if (S.mode == NB_LIST) D.g32[i] = D.g32o[i];
+  } else {
+    D.xo[i] = D.x[i];
+    D.yo[i] = D.y[i];
+    D.zo[i] = D.z[i];
+    D.g64o[i] = D.g64[i];
+    if (S.mode == NB_LIST) D.g32o[i] = D.g32[i];
+  }
+}
+
 // Stand-alone drift (the first step of a run, before any fused force/drift launch).
 template <int MIXED>
 __global__ void __launch_bounds__(TILE) k_drift(Dev D, double dt) {
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
+  if (!S.active) {
+    hold_tile(D, S, tile, false);
+    return;
+  }
   const long long i = D.tile_first[tile] + threadIdx.x;
   float d2 = 0.0f;
   if ((int)threadIdx.x < D.tile_count[tile])

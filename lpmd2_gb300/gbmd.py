@@ -115,6 +115,7 @@ _SIGS = {
     "gbmd_batch_thermo": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(Thermo)]),
     "gbmd_batch_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "gbmd_batch_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "gbmd_batch_set_active": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int]),
     "gbmd_pair_forces_static": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
 }
@@ -413,6 +414,9 @@ class Batch:
         Zc = None if Z is None else np.ascontiguousarray(np.broadcast_to(Z, (n,)), dtype=np.int32)
         mc = None if mass is None else np.ascontiguousarray(np.broadcast_to(mass, (n,)), dtype=np.float64)
         _check(self.lib.gbmd_batch_set_atoms(self.h, sys, _p(pos), _p(vel), _p(Zc, _I32), _p(mc)))
+
+    def set_active(self, sys: int, active: bool):
+        _check(self.lib.gbmd_batch_set_active(self.h, sys, 1 if active else 0))
 
     def atoms(self, sys: int):
         n = int(self.natoms[sys])

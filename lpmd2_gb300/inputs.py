@@ -161,3 +161,82 @@ def lj_reduced_units(sigma: float, epsilon: float, mass: float) -> dict:
     """tau = sqrt(m sigma^2 / (eps * forcefactor)) fs; T* -> K; rho* -> atoms/A^3."""
     tau = math.sqrt(mass * sigma * sigma / (epsilon * FORCEFACTOR))
     return {"tau_fs": tau, "T_per_Tstar": epsilon / KBOLTZMANN, "rho_per_rhostar": 1.0 / sigma**3}
+
+
+# ---------------------------------------------------------------------------------------------
+# Ensembles and job streams (seeded; every array is a pure function of the seed)
+# ---------------------------------------------------------------------------------------------
+
+LJ_AR = dict(sigma=3.405, epsilon=0.0103, mass=39.948, Z=18)
+SC_CU = dict(e=0.012382, a=3.61, n=9, m=6, c=39.432, mass=63.546, Z=29)
+
+
+def fcc_count_k(n_target: float, kmin: int, kmax: int) -> int:
+    """FCC cells per edge k with 4k^3 atoms closest (in k) to n_target, clamped to [kmin, kmax]."""
+    return int(min(kmax, max(kmin, round((n_target / 4.0) ** (1.0 / 3.0)))))
+
+
+def lj_system(k: int, rho_star: float, t_star: float, seed: int) -> dict:
+    """Argon FCC k^3 cells (4k^3 atoms) at reduced density rho*, jittered by +-0.05 sigma, with
+    Maxwell-Boltzmann velocities at T*.  Real units (A, fs, amu, eV)."""
+    sigma, eps, mass = LJ_AR["sigma"], LJ_AR["epsilon"], LJ_AR["mass"]
+    a = (4.0 / rho_star) ** (1.0 / 3.0) * sigma
+    pos, L = fcc_fast(k, k, k, a)
+    pos = np.mod(jitter(pos, 0.05 * sigma, seed=seed), L)
+    m = np.full(len(pos), mass)
+    vel = maxwell_boltzmann(m, t_star * eps / KBOLTZMANN, seed=seed)
+    return dict(kind="lj", pos=pos, vel=vel, mass=m, Z=LJ_AR["Z"], L=L, natoms=len(pos), k=k, rho_star=rho_star,
+                t_star=t_star, seed=seed)
+
+
+def sc_cu_system(k: int, seed: int, T: float = 300.0, vacancies: float = 0.01) -> dict:
+    """Sutton-Chen copper: FCC k^3 cells at a = 3.61 A with a fraction of sites removed, velocities
+    at T (K)."""
+    pos, L = fcc_fast(k, k, k, SC_CU["a"])
+    if vacancies > 0:
+        pos = remove_sites(pos, vacancies, seed=seed)
+    m = np.full(len(pos), SC_CU["mass"])
+    vel = maxwell_boltzmann(m, T, seed=seed)
+    return dict(kind="sc", pos=pos, vel=vel, mass=m, Z=SC_CU["Z"], L=L, natoms=len(pos), k=k, seed=seed)
+
+
+def log_uniform(u: np.ndarray, lo: float, hi: float) -> np.ndarray:
+    return np.exp(math.log(lo) + u * (math.log(hi) - math.log(lo)))
+
+
+def lj_ensemble(nsys: int = 512, seed: int = 4, nmin: int = 256, nmax: int = 32000) -> list[dict]:
+    """Independent LJ systems: N log-uniform in [nmin, nmax] rounded to 4k^3 (k in [4, 20]),
+    rho* uniform in [0.70, 0.95], T* uniform in [0.7, 2.0]."""
+    u = uniform(seed, 3 * nsys, stream=11).reshape(nsys, 3)
+    n_target = log_uniform(u[:, 0], nmin, nmax)
+    out = []
+    for s in range(nsys):
+        k = fcc_count_k(n_target[s], 4, 20)
+        out.append(lj_system(k, 0.70 + 0.25 * u[s, 1], 0.7 + 1.3 * u[s, 2], seed=seed * 100003 + s))
+    return out
+
+
+def job_stream(njobs: int, rate: float, seed: int = 5, nmin: int = 500, nmax: int = 200000,
+               smin: int = 1000, smax: int = 20000, lj_fraction: float = 0.7) -> list[dict]:
+    """MD jobs with Poisson arrivals at `rate` jobs/s: 70 % LJ (rho*, T* as the ensemble), 30 %
+    Sutton-Chen Cu at 300 K; N log-uniform in [nmin, nmax] rounded to 4k^3; steps uniform in
+    [smin, smax].  Systems are generated lazily by materialize_job()."""
+    u = uniform(seed, 6 * njobs, stream=13).reshape(njobs, 6)
+    gaps = -np.log1p(-u[:, 0]) / rate
+    t = np.cumsum(gaps) - gaps[0]
+    n_target = log_uniform(u[:, 2], nmin, nmax)
+    jobs = []
+    for j in range(njobs):
+        kind = "lj" if u[j, 1] < lj_fraction else "sc"
+        k = fcc_count_k(n_target[j], 5, 36)
+        steps = int(smin + min(smax - smin, int(u[j, 3] * (smax - smin + 1))))
+        jobs.append(dict(id=j, kind=kind, k=k, steps=steps, arrival=float(t[j]), rho_star=0.70 + 0.25 * u[j, 4],
+                         t_star=0.7 + 1.3 * u[j, 5], seed=seed * 1000003 + j))
+    return jobs
+
+
+def materialize_job(job: dict) -> dict:
+    """Positions, velocities and box of a job from job_stream()."""
+    if job["kind"] == "lj":
+        return lj_system(job["k"], job["rho_star"], job["t_star"], seed=job["seed"])
+    return sc_cu_system(job["k"], seed=job["seed"])

@@ -1,0 +1,268 @@
+"""Job server: MD jobs that arrive over time, run as continuously formed batches on one GPU.
+
+Each job is one independent system (an LPMD run: atoms, plugins, a number of steps).  The
+scheduler admits waiting jobs whenever a batch slot and device memory are free: it packs the
+waiting jobs of one kind (same plugins) into a new gbmd batch, which runs on its own CUDA
+stream and host thread beside the batches already on the GPU, so work of jobs that arrived
+at different times overlaps on the device.  Inside a batch every advance runs to the next job
+completion (or a chunk bound); a finished job is read back and deactivated
+(gbmd_batch_set_active), and the rest of the batch runs on without it.  When every job of a
+batch is done the batch is destroyed and its memory returns to the budget.
+
+Admission is against a byte budget: a batch is admitted on an estimate of its footprint
+(`footprint`), and once created its actual device bytes replace the estimate in the ledger.
+A job whose own footprint exceeds the whole budget is rejected.
+
+The backend is duck-typed (``GbmdBackend`` below drives libgbmd); tests drive the same
+scheduler with a CPU stand-in.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import threading
+import time
+from typing import Callable
+
+import numpy as np
+
+# Device bytes per atom that do not depend on the list: FP64 state, double-buffered
+# positions and gather copies, permutation scratch, cell arrays and per-atom bookkeeping.
+BASE_BYTES_PER_ATOM = 640
+LIST_BYTES_PER_ENTRY = 4
+
+
+@dataclasses.dataclass
+class JobResult:
+    id: int
+    kind: str
+    natoms: int
+    steps: int
+    arrival: float
+    admitted: float = math.nan
+    finished: float = math.nan
+    batch: int = -1
+    pos: np.ndarray | None = None
+    vel: np.ndarray | None = None
+    thermo: dict | None = None
+    error: str | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def list_capacity(natoms: int, L, rl: float) -> int:
+    """Per-atom list capacity the engine allocates for one system (its sizing rule)."""
+    vol = float(L[0]) * float(L[1]) * float(L[2])
+    expect = 4.18879 * rl ** 3 * natoms / vol
+    return (int(math.ceil(expect * 1.35)) + 32 + 7) & ~7
+
+
+def footprint(systems: list[dict], rl: float) -> int:
+    """Estimated device bytes of one batch holding `systems` (list capacity is batch-wide)."""
+    n = sum(int(s["natoms"]) for s in systems)
+    cap = max(list_capacity(int(s["natoms"]), s["L"], rl) for s in systems)
+    return int(n * (BASE_BYTES_PER_ATOM + LIST_BYTES_PER_ENTRY * cap))
+
+
+class Server:
+    def __init__(self, backend, budget_bytes: float = 150e9, max_batches: int = 8, max_systems: int = 512,
+                 chunk_steps: int = 5000, clock: Callable[[], float] = time.monotonic):
+        self.backend = backend
+        self.budget = float(budget_bytes)
+        self.max_batches = int(max_batches)
+        self.max_systems = int(max_systems)
+        self.chunk_steps = int(chunk_steps)
+        self.clock = clock
+        self.used = 0.0
+        self.peak_used = 0.0
+        self.batches_started = 0
+        self._cv = threading.Condition()
+        self._running: dict[int, threading.Thread] = {}
+        self._errors: list[BaseException] = []
+
+    # ------------------------------------------------------------------ scheduler
+    def serve(self, jobs: list[dict], materialize: Callable[[dict], dict]) -> list[JobResult]:
+        """Runs `jobs` (dicts with id, kind, steps, arrival in seconds from the start) to
+        completion; `materialize(job)` gives its system (pos, vel, mass, Z, L, natoms).
+
+        The systems are the requests' payloads, which clients bring with them: they are made
+        before the clock starts, and a job enters the queue at its arrival time."""
+        systems = {j["id"]: materialize(j) for j in jobs}
+        t0 = self.clock()
+        now = lambda: self.clock() - t0  # noqa: E731
+        future = sorted(jobs, key=lambda j: (j["arrival"], j["id"]))
+        waiting: list[tuple[dict, dict]] = []
+        results: dict[int, JobResult] = {}
+        with self._cv:
+            while True:
+                t = now()
+                while future and future[0]["arrival"] <= t:
+                    job = future.pop(0)
+                    system = systems[job["id"]]
+                    res = JobResult(job["id"], job["kind"], int(system["natoms"]), int(job["steps"]),
+                                    job["arrival"])
+                    results[job["id"]] = res
+                    if footprint([system], self.backend.list_radius(job["kind"])) > self.budget:
+                        res.error = "job footprint exceeds the whole device memory budget"
+                        res.admitted = res.finished = t
+                        continue
+                    waiting.append((job, system))
+                if self._errors:
+                    # stop admitting; surface the failure once every running batch has ended
+                    if not self._running:
+                        raise self._errors[0]
+                else:
+                    self._admit(waiting, results, now)
+                    if not future and not waiting and not self._running:
+                        break
+                timeout = 0.05
+                if future:
+                    timeout = max(0.0, min(timeout, future[0]["arrival"] - now()))
+                self._cv.wait(timeout)
+        if self._errors:
+            raise self._errors[0]
+        return [results[j["id"]] for j in jobs]
+
+    def _admit(self, waiting, results, now):
+        while waiting and len(self._running) < self.max_batches:
+            kind = waiting[0][0]["kind"]
+            rl = self.backend.list_radius(kind)
+            picked: list[tuple[dict, dict]] = []
+            for job, system in waiting:
+                if job["kind"] != kind or len(picked) >= self.max_systems:
+                    continue
+                trial = [s for _, s in picked] + [system]
+                if self.used + footprint(trial, rl) <= self.budget:
+                    picked.append((job, system))
+            if not picked:
+                return  # the oldest kind does not fit yet: wait for memory
+            for p in picked:
+                waiting.remove(p)
+            est = footprint([s for _, s in picked], rl)
+            self.used += est
+            self.peak_used = max(self.peak_used, self.used)
+            bid = self.batches_started
+            self.batches_started += 1
+            t = now()
+            for job, _ in picked:
+                results[job["id"]].admitted = t
+                results[job["id"]].batch = bid
+            th = threading.Thread(target=self._run_batch, args=(bid, kind, picked, est, results, now), daemon=True)
+            self._running[bid] = th
+            th.start()
+
+    # ------------------------------------------------------------------ one batch
+    def _run_batch(self, bid, kind, picked, est, results, now):
+        held = est
+        handle = None
+        try:
+            handle = self.backend.open(kind, [s for _, s in picked])
+            real = self.backend.device_bytes(handle)
+            with self._cv:
+                self.used += real - held
+                held = real
+                self.peak_used = max(self.peak_used, self.used)
+            remaining = [int(job["steps"]) for job, _ in picked]
+            active = set(range(len(picked)))
+            while active:
+                n = min(min(remaining[k] for k in active), self.chunk_steps)
+                self.backend.advance(handle, n)
+                for k in active:
+                    remaining[k] -= n
+                for k in sorted(k for k in active if remaining[k] == 0):
+                    pos, vel, thermo = self.backend.read(handle, k)
+                    r = results[picked[k][0]["id"]]
+                    r.pos, r.vel, r.thermo = pos, vel, thermo
+                    r.finished = now()
+                    active.discard(k)
+                    if active:
+                        self.backend.retire(handle, k)
+        except BaseException as e:  # surfaced by serve()
+            with self._cv:
+                self._errors.append(e)
+        finally:
+            if handle is not None:
+                try:
+                    self.backend.close(handle)
+                except BaseException as e:
+                    with self._cv:
+                        self._errors.append(e)
+            with self._cv:
+                self.used -= held
+                self._running.pop(bid, None)
+                self._cv.notify_all()
+
+
+def summarize(results: list[JobResult], wall_s: float) -> dict:
+    ok = [r for r in results if r.error is None]
+    lat = np.array([r.latency for r in ok]) if ok else np.array([math.nan])
+    work = sum(r.natoms * r.steps for r in ok)
+    return {"jobs": len(results), "completed": len(ok), "rejected": len(results) - len(ok),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "atom_steps": int(work), "wall_s": wall_s, "atom_steps_per_s": work / wall_s if wall_s > 0 else math.nan}
+
+
+# ---------------------------------------------------------------------- libgbmd backend
+class GbmdBackend:
+    """Runs batches through libgbmd (mixed precision, Verlet lists, 10-step graph blocks)."""
+
+    def __init__(self, device: int = 0, precision: str = "mixed", graph_block: int = 10, lj_skin_sigma: float = 0.3,
+                 sc_skin: float = 0.5):
+        from . import gbmd
+        from . import inputs as I
+
+        self.gbmd, self.I = gbmd, I
+        self.device = device
+        self.precision = precision
+        self.graph_block = graph_block
+        sigma = I.LJ_AR["sigma"]
+        self.lj = dict(rc=2.5 * sigma, skin=lj_skin_sigma * sigma,
+                       dt=0.005 * I.lj_reduced_units(sigma, I.LJ_AR["epsilon"], I.LJ_AR["mass"])["tau_fs"])
+        self.sc = dict(rc=2.0 * I.SC_CU["a"], skin=sc_skin, dt=2.0)
+
+    def list_radius(self, kind: str) -> float:
+        p = self.lj if kind == "lj" else self.sc
+        return p["rc"] + p["skin"]
+
+    def plugins(self, kind: str):
+        g, I = self.gbmd, self.I
+        if kind == "lj":
+            p = self.lj
+            pot = g.Plugin("lennardjones", f"sigma {I.LJ_AR['sigma']} epsilon {I.LJ_AR['epsilon']} cutoff {p['rc']!r}")
+        else:
+            p = self.sc
+            c = I.SC_CU
+            pot = g.Plugin("suttonchen", f"e {c['e']} a {c['a']} n {c['n']} m {c['m']} c {c['c']} cutoff {p['rc']!r}")
+        cm = g.Plugin("verletlist", f"cutoff {p['rc']!r} skin {p['skin']!r} maxneighbors 512")
+        return cm, pot, g.Plugin("velocityverlet", f"dt {p['dt']!r}")
+
+    def open(self, kind: str, systems: list[dict]):
+        b = self.gbmd.Batch([s["natoms"] for s in systems], [s["L"] for s in systems], device=self.device)
+        for k, s in enumerate(systems):
+            b.set_atoms(k, s["pos"], s["vel"], Z=s["Z"], mass=s["mass"])
+        cm, pot, integ = self.plugins(kind)
+        b.set_cell_manager(cm)
+        b.add_potential(pot)
+        b.set_integrator(integ)
+        b.set_precision(self.precision)
+        b.set_option("graph_block", self.graph_block)
+        b.update_forces()
+        return b
+
+    def device_bytes(self, b) -> int:
+        return int(b.stats()["device_bytes"])
+
+    def advance(self, b, n: int):
+        b.do_steps(n)
+
+    def read(self, b, k: int):
+        pos, vel, _ = b.atoms(k)
+        return pos, vel, b.thermo(k)
+
+    def retire(self, b, k: int):
+        b.set_active(k, False)
+
+    def close(self, b):
+        b.close()

@@ -150,7 +150,7 @@ def cpu_sample(seconds_target: float = 15.0, procs: int | None = None) -> dict:
     ncores = procs or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     with ctx.Pool(ncores) as pool:
-        res = pool.map(_cpu_worker, [seconds_target / 3.0] * ncores)
+        res = pool.map(_cpu_worker, [seconds_target] * ncores)
     steps = sum(r[0] for r in res)
     atoms = res[0][1]
     wall = max(r[2] for r in res)
@@ -180,8 +180,11 @@ def _cpu_worker(budget: float):
                                         cm_args, pots, w["dt"], k)
     t0 = time.perf_counter()
     run(1)
-    one = time.perf_counter() - t0
-    k = max(2, int(budget / max(one, 1e-3)))
+    t1 = time.perf_counter()
+    run(3)
+    t3 = time.perf_counter()
+    per_step = max((t3 - t1) - (t1 - t0), 0.5 * (t1 - t0)) / 2.0  # without the set-up cost
+    k = max(2, int(budget / max(per_step, 1e-4)))
     t0 = time.perf_counter()
     run(k)
     dt = time.perf_counter() - t0
@@ -194,7 +197,7 @@ def run_reference_arm(args):
         return
     w = workload()
     t0 = time.perf_counter()
-    cb = cpu_sample(seconds_target=float(os.environ.get("GBMD_CPU_SECONDS", "20")))
+    cb = cpu_sample(seconds_target=float(os.environ.get("GBMD_CPU_SECONDS", "12")))
     out = {
         "metric": "atom-steps/s", "value": cb["value"], "unit": "atom-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w["natoms"] / cb["value"],
@@ -221,6 +224,11 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short direct-launch run of the workload for ncu (no timing, no JSON)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
+    ap.add_argument("--drift-steps", type=int, default=2000, help="NVE steps of the drift comparison")
+    ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched ensemble (0: skip)")
+    ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
+    ap.add_argument("--serve-jobs", type=int, default=32, help="jobs of the served stream (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, jobs/s")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -323,11 +331,16 @@ def main():
         slope = np.polyfit(t_ps, th_log[:, 3], 1)[0]  # eV per ps
         drift = float(slope * 1e3 / N)  # eV/atom/ns
 
+    drift_cmp = measure_drift(w_melt, local, args.drift_steps) if args.drift_steps > 0 else None
+    eam = eam_metal(local, args.eam_steps) if args.eam_steps > 0 else None
+    batched = batched_ensemble(local, args.batch_steps, rank=rank, world=world, dist=dist) if args.batch_steps > 0 else None
+    served = served_stream(local, args.serve_jobs, args.serve_rate, rank, world, dist) if args.serve_jobs > 0 else None
+
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu:
-        cpu = cpu_sample(seconds_target=float(os.environ.get("GBMD_CPU_SECONDS", "15")))
+        cpu = cpu_sample(seconds_target=float(os.environ.get("GBMD_CPU_SECONDS", "12")))
     launches = stats1["kernel_launches"] - stats0["kernel_launches"]
     out = {
         "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
@@ -343,6 +356,10 @@ def main():
         "fp64_value": value64 * world, "fp64_ms_per_step": ms64 / k64, "speedup_vs_fp64": value / (value64 * world),
         "force_rms_rel_err_vs_fp64": frel, "epot_rel_err_vs_fp64": abs(e_m - e_64) / abs(e_64),
         "drift_ev_per_atom_per_ns": drift,
+        "drift": drift_cmp,
+        "eam": eam,
+        "batched": batched,
+        "served": served,
         "list_rebuilds_timed": stats1["list_rebuilds"] - stats0["list_rebuilds"],
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -410,6 +427,209 @@ def end_to_end(w, device: int, chunk: int = 100, reps: int = 3) -> dict:
     return {"value": N * chunk / t, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / chunk,
             "d2h_bytes_per_step": d2h / chunk, "chunk_steps": chunk,
             "note": "per chunk: set_atoms from pinned host arrays, UpdateForces, 100 steps, thermo log and state read back"}
+
+
+def measure_drift(w, device: int, steps: int, chunk: int = 1000) -> dict:
+    """NVE total-energy drift of the mixed and the FP64 path from the same melted state: slope
+    of a linear fit of the total energy over `steps` steps, in eV/atom/ns."""
+    N = w["natoms"]
+    out = {"steps": steps, "ns": steps * w["dt"] * 1e-6}
+    for prec in ("mixed", "fp64"):
+        s = make_sim(w, prec, device=device)
+        s.update_forces()
+        s.thermo_log()
+        logs = []
+        done = 0
+        while done < steps:
+            k = min(chunk, steps - done)
+            s.do_steps(k)
+            logs.append(s.thermo_log())
+            done += k
+        log = np.concatenate(logs)
+        t_ns = log[:, 0] * w["dt"] * 1e-6
+        slope = float(np.polyfit(t_ns, log[:, 3], 1)[0]) / N
+        out[f"{prec}_ev_per_atom_per_ns"] = slope
+        out[f"{prec}_etot_rms_fluct_ev_per_atom"] = float(np.std(log[:, 3])) / N
+        s.close()
+    out["mixed_minus_fp64_ev_per_atom_per_ns"] = out["mixed_ev_per_atom_per_ns"] - out["fp64_ev_per_atom_per_ns"]
+    return out
+
+
+def lj_batch_plugins(skin_sigma: float):
+    from lpmd2_gb300 import gbmd
+
+    rc = 2.5 * SIGMA
+    dt = 0.005 * lj_tau()
+    return (gbmd.Plugin("verletlist", f"cutoff {rc!r} skin {skin_sigma * SIGMA!r} maxneighbors 512"),
+            gbmd.Plugin("lennardjones", f"sigma {SIGMA} epsilon {EPS} cutoff {rc!r}"),
+            gbmd.Plugin("velocityverlet", f"dt {dt!r}"))
+
+
+def lj_tau() -> float:
+    from lpmd2_gb300 import inputs as I
+
+    return I.lj_reduced_units(SIGMA, EPS, MASS)["tau_fs"]
+
+
+def make_batch(systems, precision: str, device: int, params: dict):
+    from lpmd2_gb300 import gbmd
+
+    b = gbmd.Batch([s["natoms"] for s in systems], [s["L"] for s in systems], device=device)
+    for k, s in enumerate(systems):
+        b.set_atoms(k, s["pos"], s["vel"], Z=s["Z"], mass=s["mass"])
+    cm, pot, integ = lj_batch_plugins(params["skin_sigma"])
+    b.set_cell_manager(cm)
+    b.add_potential(pot)
+    b.set_integrator(integ)
+    b.set_precision(precision)
+    b.set_option("graph_block", GRAPH_BLOCK)
+    b.set_option("cell_scale", params["cell_scale"])
+    return b
+
+
+def time_batch(b, device: int, warm: int, steps: int) -> float:
+    """Device ms of `steps` steps in graph blocks on the batch's stream (events around each
+    block), after `warm` untimed steps."""
+    import torch
+
+    b.update_forces()
+    b.do_steps(warm)
+    st = torch.cuda.ExternalStream(b.stream, device=device)
+    ms = 0.0
+    done = 0
+    while done < steps:
+        k = min(GRAPH_BLOCK, steps - done)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.do_steps(k)
+        e1.record(st)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        done += k
+    return ms
+
+
+def batched_ensemble(device: int, steps: int, nsys: int = 512, rank: int = 0, world: int = 1, dist=None) -> dict:
+    """The batched ensemble (512 LJ systems, N log-uniform in [256, 32000] as 4k^3, rho* in
+    [0.70, 0.95], T* in [0.7, 2.0]): autotune on a sample, then time the whole batch in both
+    precisions.  With several GPUs each rank takes its share of the systems (split by atom
+    count, no exchange) and the slowest rank's time counts."""
+    from lpmd2_gb300 import inputs as I
+    from lpmd2_gb300.autotune import tune_batch
+    from lpmd2_gb300.serve import partition
+
+    everything = I.lj_ensemble(nsys, seed=4)
+    total_atoms = sum(s["natoms"] for s in everything)
+    mine = partition([s["natoms"] for s in everything], world)[rank]
+    systems = [everything[k] for k in mine]
+    natoms = sum(s["natoms"] for s in systems)
+    t0 = time.perf_counter()
+    sample = systems[:: max(1, nsys // 64)]
+    best, trials = tune_batch(lambda p: make_batch(sample, "mixed", device, p),
+                              lambda b: time_batch(b, device, 20, 40) / 40)
+    tune_s = time.perf_counter() - t0
+    b = make_batch(systems, "mixed", device, best)
+    ms = time_batch(b, device, 20, steps)
+    st = b.stats()
+    b.close()
+    k64 = max(GRAPH_BLOCK, steps // 5 // GRAPH_BLOCK * GRAPH_BLOCK)
+    b64 = make_batch(systems, "fp64", device, best)
+    ms64 = time_batch(b64, device, GRAPH_BLOCK, k64)
+    b64.close()
+    ms, ms64 = allmax(dist, ms), allmax(dist, ms64)
+    value = total_atoms * steps / (ms * 1e-3)
+    value64 = total_atoms * k64 / (ms64 * 1e-3)
+    return {"workload": f"lj_ensemble_{nsys}", "systems": nsys, "natoms_total": total_atoms,
+            "systems_this_rank": len(systems), "natoms_this_rank": natoms,
+            "natoms_min": min(s["natoms"] for s in everything), "natoms_max": max(s["natoms"] for s in everything),
+            "steps": steps, "value": value, "unit": "atom-steps/s", "ms_per_step": ms / steps,
+            "fp64_value": value64, "speedup_vs_fp64": value / value64, "tuned": best, "tuning_trials": trials,
+            "tuning_s": tune_s, "device_bytes": st["device_bytes"],
+            "launch": "one launch per kernel for all systems; 10-step blocks as one CUDA graph"}
+
+
+def served_stream(device: int, njobs: int, rate: float, rank: int = 0, world: int = 1, dist=None) -> dict:
+    """Poisson job stream (70 % LJ, 30 % Sutton-Chen Cu; N log-uniform in [500, 200000];
+    steps uniform in [1000, 20000]) through the job server with a 150 GB budget per GPU.
+    With several GPUs every rank serves its share of the stream (split by atoms x steps)."""
+    from lpmd2_gb300 import inputs as I
+    from lpmd2_gb300.serve import GbmdBackend, Server, partition, summarize
+
+    everything = I.job_stream(njobs, rate, seed=5)
+    mine = partition([4 * j["k"] ** 3 * j["steps"] for j in everything], world)[rank]
+    jobs = [everything[k] for k in mine]
+    srv = Server(GbmdBackend(device=device), budget_bytes=150e9, max_batches=8, max_systems=512)
+    barrier(dist)
+    t0 = time.perf_counter()
+    res = srv.serve(jobs, I.materialize_job)
+    wall = time.perf_counter() - t0
+    if dist is not None:
+        gathered = [None] * world
+        dist.all_gather_object(gathered, [(r.natoms, r.steps, r.arrival, r.finished, r.error) for r in res])
+        from lpmd2_gb300.serve import JobResult
+
+        res = [JobResult(0, "", n, st, a, finished=f, error=e) for part in gathered for (n, st, a, f, e) in part]
+        wall = allmax(dist, wall)
+    out = summarize(res, wall)
+    out.update({"rate_jobs_per_s": rate, "budget_bytes": 150e9, "batches": srv.batches_started,
+                "peak_budget_used_bytes": srv.peak_used,
+                "note": "latency = completion - arrival, wall clock; payloads generated before the clock starts"})
+    return out
+
+
+def eam_metal(device: int, steps: int, ncell: int = 50) -> dict:
+    """Sutton-Chen copper: FCC 50^3 at a = 3.61 A with 1 % of the sites removed (495,000 atoms),
+    300 K, linkedcell nx 25 (cell edge = cutoff = 7.22 A), velocityverlet dt 2 fs.  Mixed and
+    FP64 throughput, and the mixed path's force RMS, energy and virial-pressure errors against
+    FP64 at the same state."""
+    from lpmd2_gb300 import gbmd
+    from lpmd2_gb300 import inputs as I
+
+    w = I.sc_cu_system(ncell, seed=3)
+    c = I.SC_CU
+    N = w["natoms"]
+    nx = int(round(w["L"][0] / (2 * c["a"])))
+
+    def make(prec, state):
+        sim = gbmd.Simulation(N, w["L"], device=device)
+        sim.set_atoms(state["pos"], state["vel"], Z=w["Z"], mass=w["mass"])
+        sim.set_cell_manager(gbmd.Plugin("linkedcell", f"cutoff {2 * c['a']!r} nx {nx} ny {nx} nz {nx}"))
+        sim.add_potential(gbmd.Plugin("suttonchen", f"e {c['e']} a {c['a']} n {c['n']} m {c['m']} c {c['c']} "
+                                                    f"cutoff {2 * c['a']!r}"))
+        sim.set_integrator(gbmd.Plugin("velocityverlet", "dt 2.0"))
+        sim.set_precision(prec)
+        sim.set_option("graph_block", GRAPH_BLOCK)
+        return sim
+
+    # time the mixed path from the lattice; its final (thermalised) state is where the
+    # errors are measured: on the perfect lattice the forces nearly cancel
+    sm = make("mixed", w)
+    ms = time_batch(sm, device, 20, steps)
+    st = sm.stats()
+    pos, vel, _ = sm.atoms()
+    sm.close()
+    hot = dict(w, pos=pos, vel=vel)
+    sm, s64 = make("mixed", hot), make("fp64", hot)
+    sm.update_forces()
+    s64.update_forces()
+    am, a64 = sm.atoms()[2], s64.atoms()[2]
+    tm, t64 = sm.thermo(), s64.thermo()
+    frel = float(np.sqrt(np.sum((am - a64) ** 2) / np.sum(a64 ** 2)))
+    sm.close()
+    k64 = max(GRAPH_BLOCK, steps // 5 // GRAPH_BLOCK * GRAPH_BLOCK)
+    ms64 = time_batch(s64, device, GRAPH_BLOCK, k64)
+    s64.close()
+    value, value64 = N * steps / (ms * 1e-3), N * k64 / (ms64 * 1e-3)
+    return {"workload": "sc_cu_fcc50_vac1pct", "natoms": N, "steps": steps, "value": value, "unit": "atom-steps/s",
+            "ms_per_step": ms / steps, "ns_per_day": value / N * 2.0 * 86400 * 1e-6, "fp64_value": value64,
+            "speedup_vs_fp64": value / value64, "force_rms_rel_err_vs_fp64": frel,
+            "epot_rel_err_vs_fp64": abs(tm["potential_energy"] - t64["potential_energy"]) / abs(t64["potential_energy"]),
+            "virial_pressure_rel_err_vs_fp64": abs(tm["virial_pressure"] - t64["virial_pressure"])
+            / abs(t64["virial_pressure"]),
+            "epot_ev": t64["potential_energy"], "virial_pressure_mpa": t64["virial_pressure"],
+            "errors_at": f"the state after {20 + steps} mixed steps from the lattice",
+            "neighbor_mode": st["neighbor_mode"], "list_radius": st["list_radius"]}
 
 
 if __name__ == "__main__":

@@ -165,8 +165,15 @@ gbmd_status gbmd_sim_add_potential(gbmd_sim* sim, const gbmd_plugin* potential, 
 /* Simulation::SetIntegrator (liblpmd/lpmd/simulation.h:37). */
 gbmd_status gbmd_sim_set_integrator(gbmd_sim* sim, const gbmd_plugin* integrator);
 gbmd_status gbmd_sim_set_precision(gbmd_sim* sim, int precision);
-/* Tuning/behaviour options as text key/value pairs (e.g. "skin", "graph_block",
- * "thermo_every", "atoms_per_warp", "cell_scale").  Unknown keys are GBMD_ERR_INVALID. */
+/* Tuning/behaviour options as text key/value pairs.  Unknown keys are GBMD_ERR_INVALID.
+ *   "skin"             Verlet skin in A (overrides the cell manager's)
+ *   "cell_scale"       1: list-build cells >= cutoff+skin (27-cell stencil), 2: half that (125)
+ *   "graph_block"      steps per captured CUDA graph (default 10)
+ *   "graph_mode"       0 direct launches, 1 graphs, 2 graphs with a device-decided rebuild (default)
+ *   "maxneighbors_cap" verletlist maxneighbors (PluginError when reached)
+ *   "time_kernels"     1: CUDA-event timing of every kernel class (graph_mode 0), see gbmd_stats
+ *   "stream_priority"  1: the highest stream priority, 0: the lowest (default); replaces the
+ *                      stream, so read gbmd_*_stream afterwards */
 gbmd_status gbmd_sim_set_option(gbmd_sim* sim, const char* key, const char* value);
 
 /* CombinedPotential::UpdateForces (liblpmd/lpmd/combinedpotential.h:39-52): zeroes

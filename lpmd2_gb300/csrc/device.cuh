@@ -110,6 +110,12 @@ struct Dev {
   int* ncount;
   int maxnb;
   int *cstart, *ccnt, *ccount, *ccursor, *acell, *perm;
+  int* cell_sys;     // system of each cell (flat cell index over every system)
+  double* ccentre;   // cell centres (x, y, z per flat cell index) of Verlet-list grids
+  int total_cells;
+  int* lblk_sys;     // list-build blocks: system and first flat cell of each block
+  int* lblk_cell;
+  int list_blocks;
   // permutation scratch
   double* sdbl;   // 11*N doubles
   int* sint;      // 4*N ints
@@ -167,8 +173,14 @@ __device__ __forceinline__ double ref_sq(double x, double y, double z) {
 }
 
 // One axis of OrthogonalCell::FittedInside (liblpmd/lpmd/orthogonalcell.h:102-114).
+// The test (v < 0.0 || v > L) is decided on the bit patterns with integer compares instead of
+// two compares on GB300's scarce FP64 pipe: v < 0 <=> sign bit set and v is not -0.0; for
+// v >= +0, v > L <=> bits(v) > bits(L).  (A NaN is wrapped here and not in the reference; it
+// stays NaN either way.)
 __device__ __forceinline__ double ref_fitted(double v, double L) {
-  if (v < 0.0 || v > L) v = dsub(v, dmul(L, floor(ddiv(v, L))));
+  const long long b = __double_as_longlong(v);
+  if ((b < 0 && b != (long long)0x8000000000000000ULL) || b > __double_as_longlong(L))
+    v = dsub(v, dmul(L, floor(ddiv(v, L))));
   return v;
 }
 

@@ -486,6 +486,30 @@ struct Engine::Impl {
     CK(cudaStreamSynchronize(stream));
   }
 
+  // Re-creates the two streams at the device's highest (high = 1) or lowest (0) priority:
+  // when SM slots free up, blocks of high-priority streams are scheduled first, so a small
+  // batch sharing the GPU with a large one keeps a short step latency.  Graph executables
+  // are not bound to a stream and survive.
+  void set_priority(int high) {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaStreamSynchronize(stream2));
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = high ? greatest : least;
+    cudaStream_t a = nullptr, b = nullptr;
+    CK(cudaStreamCreateWithPriority(&a, cudaStreamNonBlocking, prio));
+    cudaError_t e = cudaStreamCreateWithPriority(&b, cudaStreamNonBlocking, prio);
+    if (e != cudaSuccess) {
+      cudaStreamDestroy(a);
+      ck(e, "cudaStreamCreateWithPriority");
+    }
+    cudaStreamDestroy(stream);
+    cudaStreamDestroy(stream2);
+    stream = a;
+    stream2 = b;
+  }
+
   void upload_sysd() {
     CK(cudaMemcpyAsync(d_sysd, sysd.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, stream));
   }
@@ -614,10 +638,7 @@ struct Engine::Impl {
         throw Error(1, "every system of a batch must use the same neighbour mode (box too small for a Verlet list?)");
     // cell arrays and neighbour list
     free_cells();
-    D.cstart = alloc<int>(total_cells, true);
-    D.ccnt = alloc<int>(total_cells, true);
-    D.ccount = alloc<int>(total_cells, true);
-    D.ccursor = alloc<int>(total_cells, true);
+    alloc_cells(total_cells);
     int maxnb = 0;
     if (any_list) {
       maxnb = (int)std::ceil(max_expect * 1.35) + 32;
@@ -625,11 +646,40 @@ struct Engine::Impl {
     }
     alloc_list(maxnb);
     upload_sysd();
+    k_cell_centres<<<nblocks(total_cells, 256), 256, 0, stream>>>(D);  // reads the uploaded grids
     k_clear_state<<<nblocks(nsys, 128), 128, 0, stream>>>(D, nsys);
-    launched();
+    launched(2);
     check_launch("clear");
     configured = true;
     forces_valid = false;
+  }
+
+  // Cell arrays of the current grids (sysd[*].cell_base / ncells) and the per-cell system map.
+  void alloc_cells(int total) {
+    D.cstart = alloc<int>(total, true);
+    D.ccnt = alloc<int>(total, true);
+    D.ccount = alloc<int>(total, true);
+    D.ccursor = alloc<int>(total, true);
+    std::vector<int> cs(total);
+    for (int q = 0; q < nsys; ++q)
+      for (int c = 0; c < sysd[q].ncells; ++c) cs[sysd[q].cell_base + c] = q;
+    D.cell_sys = alloc<int>(total, true);
+    CK(cudaMemcpyAsync(D.cell_sys, cs.data(), sizeof(int) * total, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    D.total_cells = total;
+    D.ccentre = alloc<double>(3 * (size_t)total, true);
+    std::vector<int> bs, bc;
+    for (int q = 0; q < nsys; ++q)
+      for (int c = 0; c < sysd[q].ncells; c += LIST_WARPS) {
+        bs.push_back(q);
+        bc.push_back(sysd[q].cell_base + c);
+      }
+    D.list_blocks = (int)bs.size();
+    D.lblk_sys = alloc<int>(bs.size(), true);
+    D.lblk_cell = alloc<int>(bc.size(), true);
+    CK(cudaMemcpyAsync(D.lblk_sys, bs.data(), sizeof(int) * bs.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(D.lblk_cell, bc.data(), sizeof(int) * bc.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
   }
 
   void alloc_list(int maxnb) {
@@ -662,14 +712,12 @@ struct Engine::Impl {
     k_bin<<<nb, 256, 0, s>>>(D);
     k_scan<<<nsys, 1024, 0, s>>>(D);
     k_scatter<<<nb, 256, 0, s>>>(D);
-    int maxcells = 0;
-    for (const auto& S : sysd) maxcells = std::max(maxcells, S.ncells);
-    k_cellsort<<<dim3(nblocks(maxcells, 4), nsys), 128, 0, s>>>(D);
+    k_cellsort<<<nblocks(D.total_cells, 4), 128, 0, s>>>(D);
     k_permute<<<nb, 256, 0, s>>>(D);
     k_copyback<<<nb, 256, 0, s>>>(D);
     launched(6);
     if (any_list) {
-      k_buildlist<<<dim3(nblocks(maxcells, LIST_WARPS), nsys), 32 * LIST_WARPS, 0, s>>>(D);
+      k_buildlist<<<D.list_blocks, 32 * LIST_WARPS, 0, s>>>(D);
       launched();
     }
     mark_end(s, T_REBUILD);
@@ -690,6 +738,7 @@ struct Engine::Impl {
       StepParams sp;
       sp.dt = integ.dt;
       sp.half_dt = 0.5 * integ.dt;
+      sp.half_dt2 = 0.5 * integ.dt * integ.dt;
       sp.epi = epi;
       sp.first = (p == 0);
       sp.last = (p == np - 1);
@@ -837,9 +886,9 @@ struct Engine::Impl {
     set_buffers(cbuf);
     mark_begin(s, T_DRIFT);
     if (precision == PREC_MIXED)
-      k_drift<1><<<ntiles, TILE, 0, s>>>(D, integ.dt);
+      k_drift<1><<<ntiles, TILE, 0, s>>>(D, integ.dt, 0.5 * integ.dt * integ.dt);
     else
-      k_drift<0><<<ntiles, TILE, 0, s>>>(D, integ.dt);
+      k_drift<0><<<ntiles, TILE, 0, s>>>(D, integ.dt, 0.5 * integ.dt * integ.dt);
     mark_end(s, T_DRIFT);
     launched();
     pend = true;
@@ -1129,6 +1178,10 @@ void Engine::set_option(const std::string& key, const std::string& value) {
     I.time_kernels = (int)v;
     return;
   }
+  if (key == "stream_priority") {  // 1: highest, 0: lowest (default); replaces the stream
+    I.set_priority(v != 0.0 ? 1 : 0);
+    return;
+  }
   if (key == "skin") {
     I.opt_skin = v;
   } else if (key == "graph_block") {
@@ -1283,10 +1336,7 @@ void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* orde
     S.cell_base = total;
     total += S.ncells;
   }
-  I.D.cstart = I.alloc<int>(total, true);
-  I.D.ccnt = I.alloc<int>(total, true);
-  I.D.ccount = I.alloc<int>(total, true);
-  I.D.ccursor = I.alloc<int>(total, true);
+  I.alloc_cells(total);
   I.D.nl = nullptr;
   bool any_list = I.any_list;
   I.any_list = false;

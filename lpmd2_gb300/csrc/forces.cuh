@@ -113,7 +113,7 @@ __device__ __forceinline__ float finish_atom(const Dev& D, const SysDev& S, long
     py = dmul(vy, m);
     pz = dmul(vz, m);
   }
-  if (sp.epi == EPI_KICK_DRIFT) return drift_atom<MIXED>(D, S, i, sp.dt, vx, vy, vz, ax, ay, az);
+  if (sp.epi == EPI_KICK_DRIFT) return drift_atom<MIXED>(D, S, i, sp.dt, sp.half_dt2, vx, vy, vz, ax, ay, az);
   return 0.0f;
 }
 

@@ -32,6 +32,7 @@ enum EpiMode { EPI_FORCES = 0, EPI_KICK = 1, EPI_KICK_DRIFT = 2 };
 struct StepParams {
   double dt;
   double half_dt;       // 0.5 * dt, as AdvanceVelocity computes it
+  double half_dt2;      // 0.5 * dt * dt (mixed drift)
   int epi;              // EpiMode of the final force pass
   int first;            // first potential pass of this evaluation (overwrite partials)
   int last;             // last potential pass (write accelerations)
@@ -171,14 +172,13 @@ __global__ void k_scatter(Dev D) {
 // One warp per cell (grid.y = system): orders the cell's slots by original index, the order in
 // which LinkedCell's head/next lists visit them.  Up to 32 atoms: each lane ranks its atom by
 // counting smaller tags across the warp; larger cells fall back to an insertion sort by lane 0.
+// One warp per cell over the cells of every system (flat index g; cell_sys maps it back).
 __global__ void k_cellsort(Dev D) {
-  const int s = blockIdx.y;
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= D.total_cells) return;
+  const int s = D.cell_sys[g];
   if (!D.sst[s].need_rebuild) return;
-  const SysDev& S = D.sysd[s];
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (c >= S.ncells) return;
   const int lane = threadIdx.x & 31;
-  const int g = S.cell_base + c;
   const int b = D.cstart[g], n = D.ccnt[g];
   if (n <= 32) {
     int v = lane < n ? D.perm[b + lane] : 0;
@@ -231,11 +231,11 @@ __global__ void k_permute(Dev D) {
   if (D.has_flags) D.sflags[p] = D.flags[o];
 }
 
-// Offset of x from the centre of cell coordinate c (edge d), wrapped into [-L/2, L/2).  Four
-// FP64-pipe operations on the common path (the FP64 unit is GB300's scarcest); the wrap is
-// only taken for atoms far from their home cell (outside the box in the input).
-__device__ __forceinline__ float home_offset(double x, int c, double d, double L, double Lh) {
-  double o = x - fma((double)c, d, 0.5 * d);
+// Offset of x from the centre xc of its home cell, wrapped into [-L/2, L/2).  Two FP64-pipe
+// operations on the common path (the FP64 unit is GB300's scarcest); the wrap is only taken
+// for atoms far from their home cell (outside the box in the input).
+__device__ __forceinline__ float home_offset(double x, double xc, double L, double Lh) {
+  double o = x - xc;
   float of = (float)o;
   if (fabsf(of) >= 0.999f * (float)Lh) {
     if (o >= Lh) o = dsub(o, L);
@@ -252,10 +252,9 @@ __device__ __forceinline__ float4 write_gather(const Dev& D, const SysDev& S, lo
   g64[p] = make_double4_32a(xx, yy, zz, (double)t);
   float4 g = make_float4(0.f, 0.f, 0.f, __int_as_float(t));
   if (S.mode == NB_LIST) {
-    int h = D.home[p] - S.cell_base;
-    int cx = h % S.n[0], cy = (h / S.n[0]) % S.n[1], cz = h / (S.n[0] * S.n[1]);
-    g = make_float4(home_offset(xx, cx, S.d[0], S.L[0], S.Lh[0]), home_offset(yy, cy, S.d[1], S.L[1], S.Lh[1]),
-                    home_offset(zz, cz, S.d[2], S.L[2], S.Lh[2]), __int_as_float(t));
+    const double* c = D.ccentre + 3 * (long long)D.home[p];
+    g = make_float4(home_offset(xx, c[0], S.L[0], S.Lh[0]), home_offset(yy, c[1], S.L[1], S.Lh[1]),
+                    home_offset(zz, c[2], S.L[2], S.Lh[2]), __int_as_float(t));
     g32[p] = g;
   }
   return g;
@@ -316,51 +315,68 @@ __device__ __forceinline__ int shift_code(int kx, int ky, int kz) { return (kx +
 // tests the staged candidate against its own atom (broadcast reads, no divergence between
 // lanes, since all atoms of a cell share the stencil and its cell-shift codes).
 constexpr int LIST_WARPS = 4;
+// Resident blocks per SM the register allocation of the list build is sized for.
+#ifndef GBMD_LIST_MIN_BLOCKS
+#define GBMD_LIST_MIN_BLOCKS 4
+#endif
 
-__global__ void __launch_bounds__(32 * LIST_WARPS) k_buildlist(Dev D) {
+__global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_buildlist(Dev D) {
   __shared__ float4 stage[LIST_WARPS][32];
-  const int s = blockIdx.y;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // every block covers LIST_WARPS cells of one system (a per-block table), so the system
+  // index is the same for the whole block and the grid holds no block of an empty range
+  const int s = D.lblk_sys[blockIdx.x];
+  const int g0 = D.lblk_cell[blockIdx.x] + w;
+  if (g0 >= D.sysd[s].cell_base + D.sysd[s].ncells) return;
   if (!D.sst[s].need_rebuild) return;
+  // the system's grid in registers: the list stores below may alias any global memory, so
+  // fields read through the SysDev reference would be re-read after every store
   const SysDev& S = D.sysd[s];
   if (S.mode != NB_LIST) return;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * LIST_WARPS + w;
-  if (c >= S.ncells) return;
-  const int g0 = S.cell_base + c;
-  const int b0 = D.cstart[g0], n0 = D.ccnt[g0];
-  const int cx = c % S.n[0], cy = (c / S.n[0]) % S.n[1], cz = c / (S.n[0] * S.n[1]);
+  const int nx = S.n[0], ny = S.n[1], nz = S.n[2];
+  const float dfx = S.df[0], dfy = S.df[1], dfz = S.df[2];
+  const int cell_base = S.cell_base;
+  const long long atom_base = S.atom_base;
+  const float rlist2 = S.rlist2f;
   const int R = S.stencil_r;
   const int na = S.natoms;
-  float4* st = stage[w];
+  unsigned* const nl = D.nl + S.nl_base;
+  const int* __restrict__ cstart = D.cstart;
+  const int* __restrict__ ccnt = D.ccnt;
+  const float4* __restrict__ g32 = D.g32;
   const int maxnb = D.maxnb;
+  const int c = g0 - cell_base;
+  const int b0 = cstart[g0], n0 = ccnt[g0];
+  const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+  float4* st = stage[w];
   for (int base = 0; base < n0; base += 32) {
     const bool has = base + lane < n0;
     const long long i = (long long)b0 + base + lane;
-    const int li = (int)(i - S.atom_base);
-    const float4 gi = has ? D.g32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float rl2 = has ? S.rlist2f : -1.0f;  // lanes without an atom never match
-    unsigned* out = D.nl + S.nl_base + (long long)li * 4;
+    const int li = (int)(i - atom_base);
+    const float4 gi = has ? g32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float rl2 = has ? rlist2 : -1.0f;  // lanes without an atom never match
+    unsigned* out = nl + (long long)li * 4;
     const long long gstride = (long long)na * 4;  // words between consecutive groups of four
     int cnt = 0;
     for (int dz = -R; dz <= R; ++dz) {
-      const int zc = wrap_around(cz + dz, S.n[2]);
-      const float sz = (float)dz * S.df[2];
+      const int zc = wrap_around(cz + dz, nz);
+      const float sz = (float)dz * dfz;
       for (int dy = -R; dy <= R; ++dy) {
-        const int yc = wrap_around(cy + dy, S.n[1]);
-        const float sy = (float)dy * S.df[1];
+        const int yc = wrap_around(cy + dy, ny);
+        const float sy = (float)dy * dfy;
         for (int dx = -R; dx <= R; ++dx) {
-          const int xc = wrap_around(cx + dx, S.n[0]);
-          const float sx = (float)dx * S.df[0];
-          const int g = S.cell_base + (zc * S.n[1] + yc) * S.n[0] + xc;
-          const int b = D.cstart[g], n = D.ccnt[g];
+          const int xc = wrap_around(cx + dx, nx);
+          const float sx = (float)dx * dfx;
+          const int g = cell_base + (zc * ny + yc) * nx + xc;
+          const int b = cstart[g], n = ccnt[g];
           const unsigned code = (unsigned)shift_code(dx, dy, dz) << CODE_SHIFT;
           const float ox = sx - gi.x, oy = sy - gi.y, oz = sz - gi.z;
           for (int jb = 0; jb < n; jb += 32) {
             __syncwarp();
-            if (jb + lane < n) st[lane] = D.g32[b + jb + lane];
+            if (jb + lane < n) st[lane] = g32[b + jb + lane];
             __syncwarp();
             const int m = min(32, n - jb);
-            const int jl0 = b + jb - (int)S.atom_base;
+            const int jl0 = b + jb - (int)atom_base;
             // pass 1: a bit per staged candidate inside the list radius (branch-free)
             unsigned hits = 0u;
             for (int k = 0; k < m; ++k) {
@@ -394,17 +410,28 @@ __global__ void __launch_bounds__(32 * LIST_WARPS) k_buildlist(Dev D) {
 // Integration: drift half of velocity Verlet
 // ---------------------------------------------------------------------------------------------
 
+// Centre of every Verlet-list cell: ((c + 1/2) * d) per axis, FP64.
+__global__ void k_cell_centres(Dev D) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= D.total_cells) return;
+  const SysDev& S = D.sysd[D.cell_sys[g]];
+  const int c = g - S.cell_base;
+  const int cx = c % S.n[0], cy = (c / S.n[0]) % S.n[1], cz = c / (S.n[0] * S.n[1]);
+  D.ccentre[3 * (long long)g] = fma((double)cx, S.d[0], 0.5 * S.d[0]);
+  D.ccentre[3 * (long long)g + 1] = fma((double)cy, S.d[1], 0.5 * S.d[1]);
+  D.ccentre[3 * (long long)g + 2] = fma((double)cz, S.d[2], 0.5 * S.d[2]);
+}
+
 // VelocityVerlet::AdvancePosition of atom i from the evaluation buffer into the output buffer:
 // newpos = x + v*dt + 0.5*a*dt*dt, then FittedInside.  The FP64 path rounds every product and
 // sum separately as the reference does; the mixed path uses two FP64 fused multiply-adds per
 // coordinate.  Returns the squared displacement since the last list build.
 template <int MIXED>
-__device__ __forceinline__ float drift_atom(const Dev& D, const SysDev& S, long long i, double dt, double vx,
-                                            double vy, double vz, double ax, double ay, double az) {
+__device__ __forceinline__ float drift_atom(const Dev& D, const SysDev& S, long long i, double dt, double h2,
+                                            double vx, double vy, double vz, double ax, double ay, double az) {
   double nx = D.x[i], ny = D.y[i], nz = D.z[i];
   if (!(D.has_flags && (D.flags[i] & FLAG_FIXEDPOS))) {
-    if (MIXED) {
-      const double h2 = 0.5 * dt * dt;
+    if (MIXED) {  // h2 = 0.5 * dt * dt
       nx = fma(h2, ax, fma(dt, vx, nx));
       ny = fma(h2, ay, fma(dt, vy, ny));
       nz = fma(h2, az, fma(dt, vz, nz));
@@ -449,7 +476,7 @@ __device__ __forceinline__ void hold_tile(const Dev& D, const SysDev& S, int til
 
 // Stand-alone drift (the first step of a run, before any fused force/drift launch).
 template <int MIXED>
-__global__ void __launch_bounds__(TILE) k_drift(Dev D, double dt) {
+__global__ void __launch_bounds__(TILE) k_drift(Dev D, double dt, double h2) {
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
@@ -460,7 +487,7 @@ __global__ void __launch_bounds__(TILE) k_drift(Dev D, double dt) {
   const long long i = D.tile_first[tile] + threadIdx.x;
   float d2 = 0.0f;
   if ((int)threadIdx.x < D.tile_count[tile])
-    d2 = drift_atom<MIXED>(D, S, i, dt, D.vx[i], D.vy[i], D.vz[i], D.ax[i], D.ay[i], D.az[i]);
+    d2 = drift_atom<MIXED>(D, S, i, dt, h2, D.vx[i], D.vy[i], D.vz[i], D.ax[i], D.ay[i], D.az[i]);
   track_displacement_warp(D, s, d2);
 }
 

@@ -67,9 +67,15 @@ def footprint(systems: list[dict], rl: float) -> int:
 
 
 class Server:
-    def __init__(self, backend, budget_bytes: float = 150e9, max_batches: int = 8, max_systems: int = 512,
-                 chunk_steps: int = 5000, clock: Callable[[], float] = time.monotonic):
+    def __init__(self, backend, budget_bytes: float = 150e9, max_batches: int = 4, max_systems: int = 512,
+                 chunk_steps: int = 5000, window_s: float = 0.2, fill_atoms: int = 2_000_000,
+                 clock: Callable[[], float] = time.monotonic):
+        """window_s / fill_atoms: a batch is formed once its oldest waiting job has waited
+        window_s, or once fill_atoms atoms of its kind are waiting (enough to fill the GPU),
+        so that jobs arriving close together share a batch instead of each taking a slot."""
         self.backend = backend
+        self.window_s = float(window_s)
+        self.fill_atoms = int(fill_atoms)
         self.budget = float(budget_bytes)
         self.max_batches = int(max_batches)
         self.max_systems = int(max_systems)
@@ -119,15 +125,26 @@ class Server:
                         break
                 timeout = 0.05
                 if future:
-                    timeout = max(0.0, min(timeout, future[0]["arrival"] - now()))
-                self._cv.wait(timeout)
+                    timeout = min(timeout, future[0]["arrival"] - now())
+                if waiting:
+                    timeout = min(timeout, min(j["arrival"] for j, _ in waiting) + self.window_s - now())
+                self._cv.wait(max(0.0, timeout))
         if self._errors:
             raise self._errors[0]
         return [results[j["id"]] for j in jobs]
 
     def _admit(self, waiting, results, now):
         while waiting and len(self._running) < self.max_batches:
-            kind = waiting[0][0]["kind"]
+            # the kind whose oldest job is ready: waited out the window, or enough atoms queued
+            kind = None
+            for k in dict.fromkeys(j["kind"] for j, _ in waiting):
+                ofk = [(j, s) for j, s in waiting if j["kind"] == k]
+                oldest = min(j["arrival"] for j, _ in ofk)
+                if now() - oldest >= self.window_s or sum(int(s["natoms"]) for _, s in ofk) >= self.fill_atoms:
+                    kind = k
+                    break
+            if kind is None:
+                return
             rl = self.backend.list_radius(kind)
             picked: list[tuple[dict, dict]] = []
             for job, system in waiting:
@@ -195,6 +212,19 @@ class Server:
                 self._cv.notify_all()
 
 
+def partition(costs, world: int) -> list[list[int]]:
+    """Indices of independent work items (systems or jobs) split over `world` GPUs by
+    estimated cost (atoms x steps): longest first onto the least loaded rank.  Deterministic,
+    so every rank computes the same split without an exchange."""
+    loads = [0.0] * world
+    parts: list[list[int]] = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda k: (-float(costs[k]), k)):
+        r = min(range(world), key=lambda q: (loads[q], q))
+        parts[r].append(i)
+        loads[r] += float(costs[i])
+    return [sorted(p) for p in parts]
+
+
 def summarize(results: list[JobResult], wall_s: float) -> dict:
     ok = [r for r in results if r.error is None]
     lat = np.array([r.latency for r in ok]) if ok else np.array([math.nan])
@@ -209,7 +239,7 @@ class GbmdBackend:
     """Runs batches through libgbmd (mixed precision, Verlet lists, 10-step graph blocks)."""
 
     def __init__(self, device: int = 0, precision: str = "mixed", graph_block: int = 10, lj_skin_sigma: float = 0.3,
-                 sc_skin: float = 0.5):
+                 sc_skin: float = 0.5, small_atoms: int = 100_000):
         from . import gbmd
         from . import inputs as I
 
@@ -217,6 +247,7 @@ class GbmdBackend:
         self.device = device
         self.precision = precision
         self.graph_block = graph_block
+        self.small_atoms = small_atoms
         sigma = I.LJ_AR["sigma"]
         self.lj = dict(rc=2.5 * sigma, skin=lj_skin_sigma * sigma,
                        dt=0.005 * I.lj_reduced_units(sigma, I.LJ_AR["epsilon"], I.LJ_AR["mass"])["tau_fs"])
@@ -248,8 +279,19 @@ class GbmdBackend:
         b.set_integrator(integ)
         b.set_precision(self.precision)
         b.set_option("graph_block", self.graph_block)
+        b.live = [int(s["natoms"]) for s in systems]
+        b.high = False
+        self._prioritise(b)
         b.update_forces()
         return b
+
+    def _prioritise(self, b):
+        """Small batches run at the highest stream priority: their short kernels then take SM
+        slots ahead of pending blocks of a large batch's kernels, instead of queueing behind
+        them for every dependent launch of a step."""
+        if not b.high and sum(b.live) <= self.small_atoms:
+            b.set_option("stream_priority", 1)
+            b.high = True
 
     def device_bytes(self, b) -> int:
         return int(b.stats()["device_bytes"])
@@ -263,6 +305,8 @@ class GbmdBackend:
 
     def retire(self, b, k: int):
         b.set_active(k, False)
+        b.live[k] = 0
+        self._prioritise(b)
 
     def close(self, b):
         b.close()

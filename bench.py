@@ -319,8 +319,12 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
-    force_bytes_per_atom = 120.0  # own position 24 + v, a_old 48 in; v, a 48 out
+    # the fused force kernel moves the step's whole compulsory state once: read x, v, a
+    # (72 B), write a, v, x (72 B), plus the force read of x counted by the 168 B/atom-step
+    # convention (x is read once here)
+    force_bytes_per_atom = 168.0
     achieved = force_bytes_per_atom * N / (kt["force_ms"] * 1e-3) / 1e9 if kt["force_ms"] else None
+    traffic = profiled_traffic("k_force32_lj_liquid_256k.md")
     step_bytes_per_atom = 168.0
     step_achieved = step_bytes_per_atom * N * args.steps / (ms * 1e-3) / 1e9
 
@@ -363,8 +367,10 @@ def main():
         "list_rebuilds_timed": stats1["list_rebuilds"] - stats0["list_rebuilds"],
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "traffic": None,
-                     "kernel": "k_force32<pair> (fused LJ force + velocity kick)",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
+                                       "(profiles/k_force32_lj_liquid_256k.md); the Verlet list dominates it",
+                     "kernel": "k_force32<pair> (fused LJ force + velocity kick + drift)",
                      "bytes_per_atom": force_bytes_per_atom, "launch_ms": kt["force_ms"],
                      "peak_source": peak_kind},
         "step_roofline": {"achieved": step_achieved, "peak": peak, "unit": "GB/s", "frac": step_achieved / peak,
@@ -427,6 +433,17 @@ def end_to_end(w, device: int, chunk: int = 100, reps: int = 3) -> dict:
     return {"value": N * chunk / t, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / chunk,
             "d2h_bytes_per_step": d2h / chunk, "chunk_steps": chunk,
             "note": "per chunk: set_atoms from pinned host arrays, UpdateForces, 100 steps, thermo log and state read back"}
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/<name> (None if absent)."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":", 1)[1])
+    return None
 
 
 def measure_drift(w, device: int, steps: int, chunk: int = 1000) -> dict:

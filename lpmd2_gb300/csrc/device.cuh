@@ -139,6 +139,7 @@ struct Dev {
   double* thermo_log;
   int log_cap;
   int has_flags;
+  int nsys;
 };
 
 // Verlet-list layout: entries are stored in groups of four (16 bytes).  Group q of the local

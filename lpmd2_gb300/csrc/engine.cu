@@ -462,6 +462,7 @@ struct Engine::Impl {
     D.sys_acc = alloc<unsigned long long>((size_t)nsys * SA_LEN);
     D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
     D.log_cap = log_cap;
+    D.nsys = nsys;
     D.thermo_log = alloc<double>((size_t)nsys * log_cap * THERMO_LEN);
     d_sysd = alloc<SysDev>(nsys);
     d_sst = alloc<SysState>(nsys);
@@ -723,7 +724,10 @@ struct Engine::Impl {
     mark_end(s, T_REBUILD);
   }
 
-  void launch_force_passes(cudaStream_t s, int epi, int count_step) {
+  // decide_next / cond_next: the mixed path's tail kernel also decides the next step's rebuild
+  // and sets that step's graph conditional (0: a k_decide launch does it instead).
+  void launch_force_passes(cudaStream_t s, int epi, int count_step, int decide_next = 0,
+                           cudaGraphConditionalHandle cond_next = 0) {
     const bool mixed = precision == PREC_MIXED;
     const int np = (int)pots.size();
     mark_begin(s, T_FORCE);
@@ -789,7 +793,10 @@ struct Engine::Impl {
       launched();
     }
     mark_end(s, T_FORCE);
-    k_thermo<<<nsys, TILE, 0, s>>>(D, mixed ? 1 : 0, count_step);
+    if (mixed)
+      k_tail<<<1, 256, 0, s>>>(D, count_step, decide_next, (unsigned long long)cond_next);
+    else
+      k_thermo<<<nsys, TILE, 0, s>>>(D, 0, count_step);
     launched();
   }
 
@@ -902,8 +909,8 @@ struct Engine::Impl {
   }
 
   // Second half: fused force + kick + drift into the other buffer; commits the step.
-  void launch_step_tail(cudaStream_t s) {
-    launch_force_passes(s, EPI_KICK_DRIFT, 1);
+  void launch_step_tail(cudaStream_t s, int decide_next = 0, cudaGraphConditionalHandle cond_next = 0) {
+    launch_force_passes(s, EPI_KICK_DRIFT, 1, decide_next, cond_next);
     cbuf = 1 - cbuf;
   }
 
@@ -926,9 +933,17 @@ struct Engine::Impl {
     int64_t saved = st.kernel_launches;
     const int cbuf0 = cbuf;
     capturing = true;
+    // mixed path: the tail kernel of step k decides step k+1, so only the first step of the
+    // graph launches k_decide
+    const bool fused = precision == PREC_MIXED;
+    int64_t base_launches = 0;
     try {
       for (int k = 0; k < nsteps; ++k) {
-        launch_step_head(stream, 2, cond, cond ? handles[k] : 0);
+        set_buffers(1 - cbuf);
+        int64_t before = st.kernel_launches;
+        if (!(fused && k > 0)) launch_decide(stream, 2, 0, cond ? handles[k] : 0, cond ? 1 : 0);
+        if (!cond) launch_rebuild(stream);
+        base_launches += st.kernel_launches - before;
         if (cond) {
           cudaStreamCaptureStatus cs;
           cudaGraph_t g;
@@ -949,7 +964,10 @@ struct Engine::Impl {
           cudaGraph_t bout;
           CK(cudaStreamEndCapture(stream2, &bout));
         }
-        launch_step_tail(stream);
+        const bool decide_next = fused && k + 1 < nsteps;
+        before = st.kernel_launches;
+        launch_step_tail(stream, decide_next ? 1 : 0, (decide_next && cond) ? handles[k + 1] : 0);
+        base_launches += st.kernel_launches - before;
       }
     } catch (...) {
       capturing = false;
@@ -970,15 +988,10 @@ struct Engine::Impl {
     gsteps = nsteps;
     gparity = cbuf0;
     graph_cond = cond;
+    graph_launches = base_launches;
   }
   bool graph_cond = false;
-
-  int64_t kernels_per_step_base() const {
-    int np = (int)pots.size();
-    int eam = 0;
-    for (const auto& p : pots) eam += (p.kind != POT_LJ);
-    return 1 /*decide*/ + np + eam + 1 /*thermo*/;
-  }
+  int64_t graph_launches = 0;  // kernels one graph launch runs, rebuild chains not included
 
   void do_steps(int64_t nsteps) {
     ensure_ready();
@@ -1009,7 +1022,7 @@ struct Engine::Impl {
         build_graph(gbe);
       while (gbe > 0 && nsteps - done >= gbe && gparity == cbuf) {
         CK(cudaGraphLaunch(gexec, stream));
-        st.kernel_launches += gbe * kernels_per_step_base() + (graph_cond ? 0 : gbe * (6 + (any_list ? 1 : 0)));
+        st.kernel_launches += graph_launches;
         done += gbe;
       }
     }

@@ -224,6 +224,71 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
 // guard band around rc^2 so the set of interacting pairs is the FP64 reference's.
 // ------------------------------------------------------------------------------------------
 
+// Thermo record of system s (one thread): SetSimulationTags' quantities from the FP64 tile
+// sums `tot` (FP64 path) or, with tot == nullptr, from the system's int64 accumulators.
+__device__ __forceinline__ void thermo_record(const Dev& D, int s, const double* tot_in, int count_step) {
+  const SysDev& S = D.sysd[s];
+  SysState& st = D.sst[s];
+  double tot[PART_D];
+  for (int k = 0; k < PART_D; ++k) tot[k] = tot_in ? tot_in[k] : 0.0;
+  double epair = tot[PD_EPAIR], vir = tot[PD_VIR];
+  double stress[9];
+  for (int k = 0; k < 9; ++k) stress[k] = tot[PD_STRESS + k];
+  if (!tot_in) {
+    const long long* acc = (const long long*)D.sys_acc + (long long)s * SA_LEN;
+    const double inv = 1.0 / FIX_E, invk = 1.0 / FIX_KE;
+    epair = (double)__ldcg(acc + SA_EPAIR) * inv;
+    vir = (double)__ldcg(acc + SA_VIR) * inv;
+    for (int k = 0; k < 9; ++k) stress[k] = (double)__ldcg(acc + SA_STRESS + k) * inv;
+    tot[PD_EEMBED] = (double)__ldcg(acc + SA_EEMBED) * inv;
+    tot[PD_KE] = (double)__ldcg(acc + SA_KE) * invk;
+    for (int k = 0; k < 3; ++k) tot[PD_PX + k] = (double)__ldcg(acc + SA_P + k) * invk;
+  }
+  if (count_step) st.step += 1;
+  const double KIN2EV = 103.64269;  // liblpmd/lpmd/properties.h:10
+  double epot = epair + tot[PD_EEMBED];
+  double kin = dmul(tot[PD_KE], KIN2EV);
+  double temp = (S.natoms == 0) ? 0.0 : ddiv(dmul(2.0 / 3.0, kin), S.kbn);
+  const double vol = S.vol, pv = S.pv;  // volume and pressfactor/volume, computed on the host
+  double r[THERMO_LEN];
+  r[0] = (double)st.step;
+  r[1] = epot;
+  r[2] = kin;
+  r[3] = epot + kin;
+  r[4] = temp;
+  r[5] = vir;
+  r[6] = tot[PD_PX];
+  r[7] = tot[PD_PX + 1];
+  r[8] = tot[PD_PX + 2];
+  r[9] = vol;
+  r[10] = dmul(dmul(pv, 1.0 / 3.0), vir);
+  r[11] = dmul(dmul(pv, 2.0 / 3.0), kin);
+  r[12] = dmul(pv, dadd(dmul(2.0 / 3.0, kin), dmul(1.0 / 3.0, vir)));
+  for (int k = 0; k < 9; ++k) r[13 + k] = stress[k];
+  double* last = D.thermo_last + (long long)s * THERMO_LEN;
+  double* log = D.thermo_log + ((long long)s * D.log_cap + (st.step % D.log_cap)) * THERMO_LEN;
+  for (int k = 0; k < THERMO_LEN; ++k) {
+    last[k] = r[k];
+    if (count_step) log[k] = r[k];
+  }
+}
+
+// Tail of a mixed force evaluation (one block for every system): the thermo records from the
+// int64 accumulators and, inside a step sequence, the next step's rebuild decision and graph
+// conditional -- one launch instead of a k_thermo and a k_decide.
+__global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_next, unsigned long long cond_next) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < D.nsys; s += blockDim.x) {
+    if (D.sysd[s].active) thermo_record(D, s, nullptr, count_step);
+    if (decide_next && decide_system(D, s, 2, 0)) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && decide_next && cond_next)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)cond_next, any ? 1u : 0u);
+}
+
 // Resident blocks per SM the register allocation of the mixed force kernel is sized for.
 #ifndef GBMD_FORCE_MIN_BLOCKS
 #define GBMD_FORCE_MIN_BLOCKS 8
@@ -470,7 +535,6 @@ __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int fi
 __global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_step) {
   const int s = blockIdx.x;
   const SysDev& S = D.sysd[s];
-  SysState& st = D.sst[s];
   if (!S.active) return;
   double v[PART_D];
   for (int k = 0; k < PART_D; ++k) v[k] = 0.0;
@@ -482,52 +546,7 @@ __global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_ste
   }
   double tot[PART_D];
   if (!mixed) block_sum<double, PART_D>(v, tot);  // block-uniform branch
-  if (threadIdx.x == 0) {
-    if (mixed)
-      for (int k = 0; k < PART_D; ++k) tot[k] = 0.0;
-    double epair = tot[PD_EPAIR], vir = tot[PD_VIR];
-    double stress[9];
-    for (int k = 0; k < 9; ++k) stress[k] = tot[PD_STRESS + k];
-    if (mixed) {
-      const long long* acc = (const long long*)D.sys_acc + (long long)s * SA_LEN;
-      const double inv = 1.0 / FIX_E, invk = 1.0 / FIX_KE;
-      epair = (double)acc[SA_EPAIR] * inv;
-      vir = (double)acc[SA_VIR] * inv;
-      for (int k = 0; k < 9; ++k) stress[k] = (double)acc[SA_STRESS + k] * inv;
-      tot[PD_EEMBED] = (double)acc[SA_EEMBED] * inv;
-      tot[PD_KE] = (double)acc[SA_KE] * invk;
-      for (int k = 0; k < 3; ++k) tot[PD_PX + k] = (double)acc[SA_P + k] * invk;
-    }
-    if (count_step) st.step += 1;
-    const double KIN2EV = 103.64269, KB = 8.6173422E-05, PRESSF = 160217.65;
-    double epot = epair + tot[PD_EEMBED];
-    double kin = dmul(tot[PD_KE], KIN2EV);
-    (void)KB;
-    double temp = (S.natoms == 0) ? 0.0 : ddiv(dmul(2.0 / 3.0, kin), S.kbn);
-    const double vol = S.vol, pv = S.pv;  // volume and pressfactor/volume, computed on the host
-    double r[THERMO_LEN];
-    r[0] = (double)st.step;
-    r[1] = epot;
-    r[2] = kin;
-    r[3] = epot + kin;
-    r[4] = temp;
-    r[5] = vir;
-    r[6] = tot[PD_PX];
-    r[7] = tot[PD_PX + 1];
-    r[8] = tot[PD_PX + 2];
-    r[9] = vol;
-    (void)PRESSF;
-    r[10] = dmul(dmul(pv, 1.0 / 3.0), vir);
-    r[11] = dmul(dmul(pv, 2.0 / 3.0), kin);
-    r[12] = dmul(pv, dadd(dmul(2.0 / 3.0, kin), dmul(1.0 / 3.0, vir)));
-    for (int k = 0; k < 9; ++k) r[13 + k] = stress[k];
-    double* last = D.thermo_last + (long long)s * THERMO_LEN;
-    double* log = D.thermo_log + ((long long)s * D.log_cap + (st.step % D.log_cap)) * THERMO_LEN;
-    for (int k = 0; k < THERMO_LEN; ++k) {
-      last[k] = r[k];
-      if (count_step) log[k] = r[k];
-    }
-  }
+  if (threadIdx.x == 0) thermo_record(D, s, mixed ? nullptr : tot, count_step);
 }
 
 }  // namespace gbmd

@@ -45,40 +45,45 @@ struct StepParams {
 // ---------------------------------------------------------------------------------------------
 
 // ucall_inc: how many emulated UpdateCell calls this evaluation stands for (verletlist "each").
+// Rebuild decision of one system for the next force evaluation (one thread): clears the
+// system's fixed-point accumulators and returns whether its cells/list are rebuilt.
+__device__ __forceinline__ int decide_system(const Dev& D, int s, int ucall_inc, int force_all) {
+  const SysDev& S = D.sysd[s];
+  SysState& st = D.sst[s];
+  if (!S.active) {
+    st.need_rebuild = 0;
+    return 0;
+  }
+  int need = force_all | st.force_rebuild;
+  if (S.mode == NB_CELLS) need = 1;
+  if (S.mode == NB_LIST) {
+    float md2 = __int_as_float((int)__ldcg(&st.maxdisp2));  // atomics of the previous launch
+    if ((S.rebuild_policy == REBUILD_SKIN || S.rebuild_policy == REBUILD_BOTH) && (double)md2 > S.thresh2)
+      need = 1;
+    if (S.rebuild_policy == REBUILD_EACH || S.rebuild_policy == REBUILD_BOTH) {
+      for (int k = 0; k < ucall_inc; ++k)
+        if (((st.ucalls + k) % S.each) == 0) need = 1;
+    }
+  }
+  st.ucalls += ucall_inc;
+  if (S.mode == NB_ALLPAIRS) need = 0;
+  for (int k = 0; k < SA_LEN; ++k) D.sys_acc[(long long)s * SA_LEN + k] = 0ull;
+  st.need_rebuild = need;
+  st.force_rebuild = 0;
+  if (need) {
+    st.maxdisp2 = 0u;
+    st.rebuilds += (S.mode == NB_LIST) ? 1 : 0;
+  }
+  return need;
+}
+
 __global__ void k_decide(Dev D, int nsys, int ucall_inc, int force_all, unsigned long long cond_handle,
                          int use_cond) {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
   __syncthreads();
-  for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
-    const SysDev& S = D.sysd[s];
-    SysState& st = D.sst[s];
-    if (!S.active) {
-      st.need_rebuild = 0;
-      continue;
-    }
-    int need = force_all | st.force_rebuild;
-    if (S.mode == NB_CELLS) need = 1;
-    if (S.mode == NB_LIST) {
-      float md2 = __int_as_float((int)st.maxdisp2);
-      if ((S.rebuild_policy == REBUILD_SKIN || S.rebuild_policy == REBUILD_BOTH) && (double)md2 > S.thresh2)
-        need = 1;
-      if (S.rebuild_policy == REBUILD_EACH || S.rebuild_policy == REBUILD_BOTH) {
-        for (int k = 0; k < ucall_inc; ++k)
-          if (((st.ucalls + k) % S.each) == 0) need = 1;
-      }
-    }
-    st.ucalls += ucall_inc;
-    if (S.mode == NB_ALLPAIRS) need = 0;
-    for (int k = 0; k < SA_LEN; ++k) D.sys_acc[(long long)s * SA_LEN + k] = 0ull;
-    st.need_rebuild = need;
-    st.force_rebuild = 0;
-    if (need) {
-      st.maxdisp2 = 0u;
-      st.rebuilds += (S.mode == NB_LIST) ? 1 : 0;
-      atomicOr(&any, 1);
-    }
-  }
+  for (int s = threadIdx.x; s < nsys; s += blockDim.x)
+    if (decide_system(D, s, ucall_inc, force_all)) atomicOr(&any, 1);
   __syncthreads();
   if (use_cond && threadIdx.x == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)cond_handle, any ? 1u : 0u);
 }

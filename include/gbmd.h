@@ -195,6 +195,17 @@ gbmd_status gbmd_sim_stats(gbmd_sim* sim, gbmd_stats* out);
 /* The cudaStream_t the simulation's kernels run on. */
 gbmd_status gbmd_sim_stream(gbmd_sim* sim, void** stream);
 
+/* Checkpoint / restore, replacing Simulation::Dump / Restore
+ * (liblpmd/simulation/simulationbuilder.cc:195-293), which write 6-significant-digit text:
+ * a binary snapshot of the complete state (atoms in device order, lists, counters, thermo
+ * log).  Load it into a simulation created and configured the same way (same atoms count and
+ * cell, cell manager, potentials, integrator, precision and options): it then continues bit
+ * for bit as the saved one would have.  A different configuration is GBMD_ERR_INVALID; a
+ * buffer smaller than gbmd_sim_checkpoint_size is GBMD_ERR_CAPACITY. */
+gbmd_status gbmd_sim_checkpoint_size(gbmd_sim* sim, size_t* bytes);
+gbmd_status gbmd_sim_checkpoint_save(gbmd_sim* sim, void* buf, size_t bytes);
+gbmd_status gbmd_sim_checkpoint_load(gbmd_sim* sim, const void* buf, size_t bytes);
+
 /* CellManager::BuildNeighborList(conf, i, nlist, full, rcut) for every atom
  * (liblpmd/lpmd/cellmanager.h:25): the j indices with r^2 < rcut^2 as the force kernels
  * see them, per atom in the caller's order (neighbour order within an atom unspecified).
@@ -236,6 +247,17 @@ gbmd_status gbmd_batch_synchronize(gbmd_batch* batch);
 gbmd_status gbmd_batch_thermo(gbmd_batch* batch, int sys, gbmd_thermo* out);
 gbmd_status gbmd_batch_stats(gbmd_batch* batch, gbmd_stats* out);
 gbmd_status gbmd_batch_stream(gbmd_batch* batch, void** stream);
+/* gbmd_sim_checkpoint_* for a whole batch. */
+gbmd_status gbmd_batch_checkpoint_size(gbmd_batch* batch, size_t* bytes);
+gbmd_status gbmd_batch_checkpoint_save(gbmd_batch* batch, void* buf, size_t bytes);
+gbmd_status gbmd_batch_checkpoint_load(gbmd_batch* batch, const void* buf, size_t bytes);
+
+/* Self-test of the failure path of the kernels' bounded waits (no counterpart in the
+ * reference): one warp waits, with the force kernel's wait routine, on an asynchronous-copy
+ * barrier that nothing completes, gives up after `polls` polls (1..2^22) and returns;
+ * *gave_up = 1 means the wait ended by its bound, the status was reported and the device
+ * stays usable.  Nothing faults, traps or hangs. */
+gbmd_status gbmd_selftest_bounded_wait(int device, int64_t polls, int* gave_up);
 
 /* ---------------------------------------------------------------------------------------- */
 /* Pair forces without device allocation                                                    */

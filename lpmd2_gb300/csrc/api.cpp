@@ -370,6 +370,11 @@ gbmd_status gbmd_potential_eval(const gbmd_plugin* p, int what, const double* ar
   return guarded([&] { potential_eval(p->spec.pot, what, args, out); });
 }
 
+gbmd_status gbmd_selftest_bounded_wait(int device, int64_t polls, int* gave_up) {
+  if (!gave_up) return fail(GBMD_ERR_INVALID, "null argument");
+  return guarded([&] { *gave_up = wait_selftest(device, (long long)polls); });
+}
+
 gbmd_status gbmd_pair_forces_static(const gbmd_plugin* p, const double* pos, int n, const double* box, double* force,
                                     double* out, void* stream) {
   if (!p || !pos || !box || !force || !out) return fail(GBMD_ERR_INVALID, "null argument");
@@ -543,6 +548,27 @@ void gbmd_batch_destroy(gbmd_batch* batch) { delete batch; }
 gbmd_status gbmd_batch_set_atoms(gbmd_batch* batch, int sys, const double* pos, const double* vel, const int32_t* Z,
                                  const double* mass) {
   BATCH_GUARD(batch->eng->set_atoms(sys, pos, vel, nullptr, Z, mass));
+}
+
+gbmd_status gbmd_sim_checkpoint_size(gbmd_sim* sim, size_t* bytes) {
+  if (!bytes) return fail(GBMD_ERR_INVALID, "null argument");
+  SIM_GUARD(*bytes = sim->eng->checkpoint_size());
+}
+gbmd_status gbmd_sim_checkpoint_save(gbmd_sim* sim, void* buf, size_t bytes) {
+  SIM_GUARD(sim->eng->checkpoint_save(buf, bytes));
+}
+gbmd_status gbmd_sim_checkpoint_load(gbmd_sim* sim, const void* buf, size_t bytes) {
+  SIM_GUARD(sim->eng->checkpoint_load(buf, bytes));
+}
+gbmd_status gbmd_batch_checkpoint_size(gbmd_batch* batch, size_t* bytes) {
+  if (!bytes) return fail(GBMD_ERR_INVALID, "null argument");
+  BATCH_GUARD(*bytes = batch->eng->checkpoint_size());
+}
+gbmd_status gbmd_batch_checkpoint_save(gbmd_batch* batch, void* buf, size_t bytes) {
+  BATCH_GUARD(batch->eng->checkpoint_save(buf, bytes));
+}
+gbmd_status gbmd_batch_checkpoint_load(gbmd_batch* batch, const void* buf, size_t bytes) {
+  BATCH_GUARD(batch->eng->checkpoint_load(buf, bytes));
 }
 
 gbmd_status gbmd_batch_set_active(gbmd_batch* batch, int sys, int active) {

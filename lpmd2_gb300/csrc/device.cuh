@@ -249,8 +249,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 
 // Waits for phase `phase` of the barrier with a bounded number of polls (each poll may suspend
 // the thread for a hardware-defined interval).  Returns false if the bound was hit.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase) {
-  for (int it = 0; it < (1 << 22); ++it)
+constexpr long long WAIT_POLLS = 1ll << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase,
+                                                  long long polls = WAIT_POLLS) {
+  for (long long it = 0; it < polls; ++it)
     if (mbar_try_wait(bar, phase)) return true;
   return false;
 }

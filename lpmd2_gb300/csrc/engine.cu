@@ -9,6 +9,8 @@
 #include <mutex>
 #include <numeric>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "forces.cuh"
 
 namespace gbmd {
@@ -60,6 +62,13 @@ int lc_auto_n(double len, double cutoff) {
 }
 
 inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// NVTX range over a host call (visible in Nsight Systems / ncu timelines; a no-op without a
+// tool attached).
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
 
 }  // namespace
 
@@ -186,6 +195,20 @@ __global__ void k_cells_out(Dev D, int s, long long* cell, long long* order) {
   order[k] = D.tag[i];
 }
 
+// Failure path of the bounded waits: one warp waits, with the force kernel's mbar_wait_bounded,
+// on an mbarrier phase that nothing completes (no arrival, no copy in flight); after `polls`
+// polls it gives up, records that in *gave_up and returns.
+__global__ void k_wait_selftest(long long polls, int* gave_up) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  const bool done = mbar_wait_bounded(&bar, 0u, polls);
+  if (threadIdx.x == 0) *gave_up = done ? 0 : 1;
+}
+
 __global__ void k_clear_state(Dev D, int nsys) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
@@ -232,8 +255,8 @@ struct Engine::Impl {
   SysDev* d_sysd = nullptr;
   SysState* d_sst = nullptr;
   int *d_tile_sys = nullptr, *d_tile_first = nullptr, *d_tile_count = nullptr;
-  std::vector<void*> allocs;
-  std::vector<void*> cell_allocs;
+  std::vector<std::pair<void*, size_t>> allocs;       // set-up pool: (pointer, bytes)
+  std::vector<std::pair<void*, size_t>> cell_allocs;  // grid pool (cells, then the list last)
   size_t bytes = 0, cell_bytes = 0;
   bool configured = false, forces_valid = false, initialized = false, flags_any = false;
   Stats st;
@@ -336,13 +359,13 @@ struct Engine::Impl {
       throw Error(6, "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e));
     }
     CK(cudaMemsetAsync(p, 0, b, stream));
-    (cellpool ? cell_allocs : allocs).push_back(p);
+    (cellpool ? cell_allocs : allocs).emplace_back(p, b);
     (cellpool ? cell_bytes : bytes) += b;
     return (T*)p;
   }
 
   void free_cells() {
-    for (void* p : cell_allocs) dev_free(p);
+    for (auto& a : cell_allocs) dev_free(a.first);
     cell_allocs.clear();
     cell_bytes = 0;
   }
@@ -524,7 +547,7 @@ struct Engine::Impl {
       cudaEventDestroy(m.b);
     }
     for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
-    for (void* p : allocs) dev_free(p);
+    for (auto& a : allocs) dev_free(a.first);
     free_cells();
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
@@ -708,6 +731,7 @@ struct Engine::Impl {
   }
 
   void launch_rebuild(cudaStream_t s) {
+    Range r("gbmd:enqueue_rebuild");
     const unsigned nb = nblocks(N, 256);
     mark_begin(s, T_REBUILD);
     k_bin<<<nb, 256, 0, s>>>(D);
@@ -858,7 +882,8 @@ struct Engine::Impl {
       for (const auto& S : sysd) old_entries += (long long)S.natoms * D.maxnb;
       cell_bytes -= sizeof(unsigned) * (size_t)(old_entries ? old_entries : 1);
       dev_free(D.nl);
-      cell_allocs.erase(std::find(cell_allocs.begin(), cell_allocs.end(), (void*)D.nl));
+      cell_allocs.erase(std::find_if(cell_allocs.begin(), cell_allocs.end(),
+                                     [&](const std::pair<void*, size_t>& a) { return a.first == (void*)D.nl; }));
       alloc_list(maxnb);
       upload_sysd();
       k_clear_state<<<nblocks(nsys, 128), 128, 0, stream>>>(D, nsys);
@@ -915,6 +940,7 @@ struct Engine::Impl {
   }
 
   void build_graph(int nsteps) {
+    Range r("gbmd:capture_graph");
     std::lock_guard<std::recursive_mutex> lk(g_dev_mu);
     drop_graph();
     CK(cudaGraphCreate(&graph, 0));
@@ -1055,6 +1081,20 @@ Engine::Engine(int device, const std::vector<int64_t>& natoms, const std::vector
 
 Engine::~Engine() { delete d_; }
 
+int wait_selftest(int device, long long polls) {
+  if (polls < 1 || polls > WAIT_POLLS) throw Error(1, "polls must be in [1, 2^22]");
+  CK(cudaSetDevice(device));
+  int* d = nullptr;
+  CK(dev_malloc(&d, sizeof(int)));
+  int h = -1;
+  k_wait_selftest<<<1, 32>>>(polls, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  dev_free(d);
+  ck(e, "wait self-test");
+  return h;
+}
+
 void Engine::set_active(int sys, bool on) {
   Impl& I = *d_;
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");
@@ -1068,6 +1108,7 @@ void Engine::set_active(int sys, bool on) {
 
 void Engine::set_atoms(int sys, const double* pos, const double* vel, const double* acc, const int32_t* Z,
                        const double* mass) {
+  Range rg("gbmd:set_atoms");
   Impl& I = *d_;
   CK(cudaSetDevice(I.device));
   I.set_buffers(I.cbuf);
@@ -1127,6 +1168,7 @@ void Engine::set_flags(int sys, const uint8_t* flags) {
 }
 
 void Engine::get_atoms(int sys, double* pos, double* vel, double* acc) {
+  Range rg("gbmd:get_atoms");
   Impl& I = *d_;
   CK(cudaSetDevice(I.device));
   I.set_buffers(I.cbuf);
@@ -1213,8 +1255,14 @@ void Engine::set_option(const std::string& key, const std::string& value) {
   I.drop_graph();
 }
 
-void Engine::update_forces() { d_->update_forces(); }
-void Engine::do_steps(int64_t nsteps) { d_->do_steps(nsteps); }
+void Engine::update_forces() {
+  Range r("gbmd:update_forces");
+  d_->update_forces();
+}
+void Engine::do_steps(int64_t nsteps) {
+  Range r("gbmd:do_steps");
+  d_->do_steps(nsteps);
+}
 void Engine::synchronize() {
   CK(cudaSetDevice(d_->device));
   CK(cudaStreamSynchronize(d_->stream));
@@ -1377,6 +1425,176 @@ void Engine::cell_sort(int sys, const int32_t n[3], int64_t* cell, int64_t* orde
   I.configured = false;
   I.forces_valid = false;
   I.forces_valid_layout = false;
+}
+
+// ------------------------------------------------------------------------------------------
+// Checkpoint / restore: the complete device state (both memory pools) and the host counters,
+// so that a restored engine continues bit for bit.  Simulation::Dump/Restore
+// (liblpmd/simulation/simulationbuilder.cc:195-293) write a 6-digit text file instead.
+// ------------------------------------------------------------------------------------------
+
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  int64_t natoms_total;
+  int32_t nsys, precision, total_cells, maxnb;
+  int32_t cbuf, pend, initialized, forces_valid, forces_valid_layout, pending_ucalls, flags_any;
+  int32_t n_allocs, n_cell_allocs, n_read_from;
+  uint64_t config_hash;
+  uint64_t body_bytes;
+  Stats st;
+};
+
+constexpr char CKPT_MAGIC[8] = {'G', 'B', 'M', 'D', 'C', 'K', 'P', '1'};
+
+uint64_t fnv(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t k = 0; k < n; ++k) h = (h ^ b[k]) * 1099511628211ull;
+  return h;
+}
+template <class T>
+uint64_t fnv_v(uint64_t h, T v) {
+  return fnv(h, &v, sizeof(v));
+}
+
+}  // namespace
+
+// Everything that determines the layout and the evolution besides the device state.
+static uint64_t config_hash(const Engine::Impl& I) {
+  uint64_t h = 1469598103934665603ull;
+  for (auto n : I.natoms) h = fnv_v(h, (int64_t)n);
+  for (const auto& c : I.cells)
+    for (double v : c) h = fnv_v(h, v);
+  h = fnv_v(h, I.precision);
+  h = fnv_v(h, I.cm.kind);
+  h = fnv_v(h, I.cm.cutoff);
+  h = fnv_v(h, I.cm.nx);
+  h = fnv_v(h, I.cm.ny);
+  h = fnv_v(h, I.cm.nz);
+  h = fnv_v(h, (int)I.cm.mode_auto);
+  h = fnv_v(h, (int64_t)I.cm.maxneighbors);
+  h = fnv_v(h, (int64_t)I.cm.each);
+  h = fnv_v(h, I.cm.skin);
+  h = fnv_v(h, I.opt_skin);
+  h = fnv_v(h, I.stencil_r);
+  h = fnv_v(h, I.integ.dt);
+  for (const auto& P : I.pots) h = fnv(h, &P, sizeof(P));  // PotParams is zero-filled before use
+  return h;
+}
+
+size_t Engine::checkpoint_size() {
+  Impl& I = *d_;
+  I.ensure_ready();
+  size_t n = sizeof(CkptHeader) + sizeof(SysDev) * I.sysd.size() + 16 * I.read_from.size();
+  for (auto& a : I.allocs) n += a.second;
+  for (auto& a : I.cell_allocs) n += a.second;
+  return n;
+}
+
+void Engine::checkpoint_save(void* buf, size_t bytes) {
+  Impl& I = *d_;
+  Range r("gbmd:checkpoint_save");
+  const size_t need = checkpoint_size();
+  if (!buf || bytes < need) throw Error(9, "checkpoint buffer too small: " + std::to_string(need) + " bytes needed");
+  CK(cudaStreamSynchronize(I.stream));
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, CKPT_MAGIC, 8);
+  h.natoms_total = I.N;
+  h.nsys = I.nsys;
+  h.precision = I.precision;
+  h.total_cells = I.total_cells;
+  h.maxnb = I.D.maxnb;
+  h.cbuf = I.cbuf;
+  h.pend = I.pend;
+  h.initialized = I.initialized;
+  h.forces_valid = I.forces_valid;
+  h.forces_valid_layout = I.forces_valid_layout;
+  h.pending_ucalls = I.pending_ucalls;
+  h.flags_any = I.flags_any;
+  h.n_allocs = (int32_t)I.allocs.size();
+  h.n_cell_allocs = (int32_t)I.cell_allocs.size();
+  h.n_read_from = (int32_t)I.read_from.size();
+  h.config_hash = config_hash(I);
+  h.body_bytes = need - sizeof(CkptHeader);
+  h.st = I.st;
+  char* o = (char*)buf;
+  std::memcpy(o, &h, sizeof(h));
+  o += sizeof(h);
+  std::memcpy(o, I.sysd.data(), sizeof(SysDev) * I.sysd.size());
+  o += sizeof(SysDev) * I.sysd.size();
+  for (const auto& kv : I.read_from) {
+    int64_t pair[2] = {kv.first, kv.second};
+    std::memcpy(o, pair, 16);
+    o += 16;
+  }
+  for (auto* pool : {&I.allocs, &I.cell_allocs})
+    for (auto& a : *pool) {
+      CK(cudaMemcpyAsync(o, a.first, a.second, cudaMemcpyDeviceToHost, I.stream));
+      o += a.second;
+    }
+  CK(cudaStreamSynchronize(I.stream));
+}
+
+void Engine::checkpoint_load(const void* buf, size_t bytes) {
+  Impl& I = *d_;
+  Range r("gbmd:checkpoint_load");
+  if (!buf || bytes < sizeof(CkptHeader)) throw Error(1, "checkpoint: truncated");
+  CkptHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, CKPT_MAGIC, 8) != 0) throw Error(1, "checkpoint: not a gbmd checkpoint");
+  if (bytes != sizeof(CkptHeader) + h.body_bytes) throw Error(1, "checkpoint: size mismatch");
+  if (h.natoms_total != I.N || h.nsys != I.nsys) throw Error(1, "checkpoint: different systems");
+  I.ensure_ready();
+  if (h.config_hash != config_hash(I) || h.precision != I.precision || h.total_cells != I.total_cells)
+    throw Error(1, "checkpoint: cell manager, potentials, integrator, precision or options differ");
+  if (h.maxnb != I.D.maxnb) {  // the saved list had grown: give this engine the same capacity
+    long long old_entries = 0;
+    for (const auto& S : I.sysd) old_entries += (long long)S.natoms * I.D.maxnb;
+    I.cell_bytes -= sizeof(unsigned) * (size_t)(old_entries ? old_entries : 1);
+    dev_free(I.D.nl);
+    I.cell_allocs.erase(std::find_if(I.cell_allocs.begin(), I.cell_allocs.end(),
+                                     [&](const std::pair<void*, size_t>& a) { return a.first == (void*)I.D.nl; }));
+    I.alloc_list(h.maxnb);
+  }
+  if (h.n_allocs != (int32_t)I.allocs.size() || h.n_cell_allocs != (int32_t)I.cell_allocs.size())
+    throw Error(1, "checkpoint: device layout differs");
+  const char* in = (const char*)buf + sizeof(h);
+  std::vector<SysDev> sysd(I.nsys);
+  std::memcpy(sysd.data(), in, sizeof(SysDev) * I.nsys);
+  in += sizeof(SysDev) * I.nsys;
+  std::map<int, long long> rf;
+  for (int k = 0; k < h.n_read_from; ++k) {
+    int64_t pair[2];
+    std::memcpy(pair, in, 16);
+    in += 16;
+    rf[(int)pair[0]] = pair[1];
+  }
+  size_t body = 0;
+  for (auto* pool : {&I.allocs, &I.cell_allocs})
+    for (auto& a : *pool) body += a.second;
+  if ((size_t)(in - (const char*)buf) + body != bytes) throw Error(1, "checkpoint: device layout differs");
+  CK(cudaSetDevice(I.device));
+  for (auto* pool : {&I.allocs, &I.cell_allocs})
+    for (auto& a : *pool) {
+      CK(cudaMemcpyAsync(a.first, in, a.second, cudaMemcpyHostToDevice, I.stream));
+      in += a.second;
+    }
+  CK(cudaStreamSynchronize(I.stream));
+  I.sysd = sysd;
+  I.read_from = rf;
+  I.cbuf = h.cbuf;
+  I.pend = h.pend != 0;
+  I.initialized = h.initialized != 0;
+  I.forces_valid = h.forces_valid != 0;
+  I.forces_valid_layout = h.forces_valid_layout != 0;
+  I.pending_ucalls = h.pending_ucalls;
+  I.flags_any = h.flags_any != 0;
+  I.D.has_flags = I.flags_any ? 1 : 0;
+  I.st = h.st;
+  I.drop_graph();
+  I.set_buffers(I.cbuf);
 }
 
 }  // namespace gbmd

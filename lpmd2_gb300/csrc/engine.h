@@ -90,6 +90,10 @@ class Engine {
   void get_atoms(int sys, double* pos, double* vel, double* acc);
   // Inactive systems are skipped by every kernel; their state is left as it was.
   void set_active(int sys, bool on);
+  // Lossless snapshot of the whole engine state; load needs an identically configured engine.
+  size_t checkpoint_size();
+  void checkpoint_save(void* buf, size_t bytes);
+  void checkpoint_load(const void* buf, size_t bytes);
 
   void set_cell_manager(const CellManagerCfg& cfg);
   void add_potential(const PotParams& p);
@@ -130,6 +134,8 @@ struct PluginSpec {
 
 PluginSpec make_plugin(const std::string& name, const std::string& args);
 void potential_eval(const PotParams& p, int what, const double* args, double* out);
+// Runs the bounded-wait failure path once (a wait nothing completes); returns 1 if it gave up.
+int wait_selftest(int device, long long polls);
 // Pair forces of one small system with no device allocation (static_forces.cu); stream is a
 // cudaStream_t.
 void pair_forces_static(const PotParams& P, const double* pos, int n, const double* box, double* force, double* out,

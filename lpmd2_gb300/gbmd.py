@@ -116,6 +116,13 @@ _SIGS = {
     "gbmd_batch_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "gbmd_batch_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "gbmd_batch_set_active": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int]),
+    "gbmd_sim_checkpoint_size": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
+    "gbmd_sim_checkpoint_save": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
+    "gbmd_sim_checkpoint_load": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
+    "gbmd_batch_checkpoint_size": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
+    "gbmd_batch_checkpoint_save": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
+    "gbmd_batch_checkpoint_load": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
+    "gbmd_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     "gbmd_pair_forces_static": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
 }
@@ -179,6 +186,13 @@ def device_count() -> int:
     c = ctypes.c_int(0)
     _check(load().gbmd_device_count(ctypes.byref(c)))
     return c.value
+
+
+def selftest_bounded_wait(polls: int = 1000, device: int = 0) -> bool:
+    """True if a kernel wait that nothing completes ended by its poll bound (see gbmd.h)."""
+    g = ctypes.c_int(-1)
+    _check(load().gbmd_selftest_bounded_wait(device, int(polls), ctypes.byref(g)))
+    return g.value == 1
 
 
 def pair_forces_static(plugin: "Plugin", pos_ptr: int, n: int, box, force_ptr: int, out_ptr: int,
@@ -278,6 +292,19 @@ def _kernel_times(st: dict) -> dict:
             "rebuild_chain_launches": st["rebuild_launches"], "list_rebuilds": st["list_rebuilds"]}
 
 
+def _checkpoint(lib, kind: str, h) -> bytes:
+    n = ctypes.c_size_t(0)
+    _check(getattr(lib, f"gbmd_{kind}_checkpoint_size")(h, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value)
+    _check(getattr(lib, f"gbmd_{kind}_checkpoint_save")(h, buf, n.value))
+    return buf.raw
+
+
+def _restore(lib, kind: str, h, data: bytes):
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    _check(getattr(lib, f"gbmd_{kind}_checkpoint_load")(h, buf, len(data)))
+
+
 class Simulation:
     """One periodic orthogonal system on one GPU."""
 
@@ -304,6 +331,14 @@ class Simulation:
         Zc = None if Z is None else np.ascontiguousarray(np.broadcast_to(Z, (self.n,)), dtype=np.int32)
         mc = None if mass is None else np.ascontiguousarray(np.broadcast_to(mass, (self.n,)), dtype=np.float64)
         _check(self.lib.gbmd_sim_set_atoms(self.h, _p(pos), _p(vel), _p(acc), _p(Zc, _I32), _p(mc)))
+
+    def checkpoint(self) -> bytes:
+        """Lossless snapshot of the whole state (gbmd_sim_checkpoint_save)."""
+        return _checkpoint(self.lib, "sim", self.h)
+
+    def restore(self, data: bytes):
+        """Loads a snapshot into this identically configured simulation."""
+        _restore(self.lib, "sim", self.h, data)
 
     def set_flags(self, flags):
         f = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
@@ -414,6 +449,12 @@ class Batch:
         Zc = None if Z is None else np.ascontiguousarray(np.broadcast_to(Z, (n,)), dtype=np.int32)
         mc = None if mass is None else np.ascontiguousarray(np.broadcast_to(mass, (n,)), dtype=np.float64)
         _check(self.lib.gbmd_batch_set_atoms(self.h, sys, _p(pos), _p(vel), _p(Zc, _I32), _p(mc)))
+
+    def checkpoint(self) -> bytes:
+        return _checkpoint(self.lib, "batch", self.h)
+
+    def restore(self, data: bytes):
+        _restore(self.lib, "batch", self.h, data)
 
     def set_active(self, sys: int, active: bool):
         _check(self.lib.gbmd_batch_set_active(self.h, sys, 1 if active else 0))

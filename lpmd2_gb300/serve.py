@@ -69,11 +69,18 @@ def footprint(systems: list[dict], rl: float) -> int:
 class Server:
     def __init__(self, backend, budget_bytes: float = 150e9, max_batches: int = 4, max_systems: int = 512,
                  chunk_steps: int = 5000, window_s: float = 0.2, fill_atoms: int = 2_000_000,
-                 clock: Callable[[], float] = time.monotonic):
+                 small_atoms: int = 0, clock: Callable[[], float] = time.monotonic):
         """window_s / fill_atoms: a batch is formed once its oldest waiting job has waited
-        window_s, or once fill_atoms atoms of its kind are waiting (enough to fill the GPU),
-        so that jobs arriving close together share a batch instead of each taking a slot."""
+        window_s, or once fill_atoms atoms of its class are waiting (enough to fill the GPU),
+        so that jobs arriving close together share a batch instead of each taking a slot.
+
+        small_atoms: jobs below this size form their own batches (0: off, the default).  A
+        batch steps in lockstep, so a small job with many steps sharing a batch with large
+        systems advances at their step time.  Measured on GB300 with the default stream, the
+        split did not pay: each extra class takes a batch slot, and a small batch's kernels
+        still wait for SM slots behind the large batches' running blocks."""
         self.backend = backend
+        self.small_atoms = int(small_atoms)
         self.window_s = float(window_s)
         self.fill_atoms = int(fill_atoms)
         self.budget = float(budget_bytes)
@@ -136,19 +143,20 @@ class Server:
     def _admit(self, waiting, results, now):
         while waiting and len(self._running) < self.max_batches:
             # the kind whose oldest job is ready: waited out the window, or enough atoms queued
-            kind = None
-            for k in dict.fromkeys(j["kind"] for j, _ in waiting):
-                ofk = [(j, s) for j, s in waiting if j["kind"] == k]
-                oldest = min(j["arrival"] for j, _ in ofk)
-                if now() - oldest >= self.window_s or sum(int(s["natoms"]) for _, s in ofk) >= self.fill_atoms:
-                    kind = k
+            cls = None
+            for c in dict.fromkeys(self._class(j, s) for j, s in waiting):
+                ofc = [(j, s) for j, s in waiting if self._class(j, s) == c]
+                oldest = min(j["arrival"] for j, _ in ofc)
+                if now() - oldest >= self.window_s or sum(int(s["natoms"]) for _, s in ofc) >= self.fill_atoms:
+                    cls = c
                     break
-            if kind is None:
+            if cls is None:
                 return
+            kind = cls[0]
             rl = self.backend.list_radius(kind)
             picked: list[tuple[dict, dict]] = []
             for job, system in waiting:
-                if job["kind"] != kind or len(picked) >= self.max_systems:
+                if self._class(job, system) != cls or len(picked) >= self.max_systems:
                     continue
                 trial = [s for _, s in picked] + [system]
                 if self.used + footprint(trial, rl) <= self.budget:
@@ -169,6 +177,10 @@ class Server:
             th = threading.Thread(target=self._run_batch, args=(bid, kind, picked, est, results, now), daemon=True)
             self._running[bid] = th
             th.start()
+
+    def _class(self, job, system) -> tuple[str, bool]:
+        """Batching class: plugin kind and whether the system is small."""
+        return job["kind"], int(system["natoms"]) < self.small_atoms
 
     # ------------------------------------------------------------------ one batch
     def _run_batch(self, bid, kind, picked, est, results, now):

@@ -131,6 +131,18 @@ def test_job_larger_than_budget_is_rejected():
     assert all(r.error is None for k, r in enumerate(res) if k != big)
 
 
+def test_size_classes_never_share_a_batch():
+    jobs = small_jobs(30, 1000.0, seed=11)
+    be = CountingBackend()
+    srv = Server(be, budget_bytes=150e9, max_batches=8, max_systems=64, small_atoms=5000)
+    res = srv.serve(jobs, fake_system)
+    check_results(jobs, res, be, srv)
+    by_batch = {}
+    for r in res:
+        by_batch.setdefault(r.batch, set()).add((r.kind, r.natoms < 5000))
+    assert all(len(v) == 1 for v in by_batch.values())
+
+
 def test_backend_failure_surfaces():
     class Failing(CountingBackend):
         def advance(self, h, n):

@@ -224,6 +224,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short direct-launch run of the workload for ncu (no timing, no JSON)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
+    ap.add_argument("--workload", default="lj", choices=["lj", "eam"], help="with --profile")
     ap.add_argument("--drift-steps", type=int, default=2000, help="NVE steps of the drift comparison")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched ensemble (0: skip)")
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
@@ -386,7 +387,17 @@ def main():
 
 def run_profile(args):
     """The workload with direct launches only (graph_mode 0), for ncu: melt, warm up, then
-    --steps steps.  Every kernel of a step is a separate launch on the simulation's stream."""
+    --steps steps.  Every kernel of a step is a separate launch on the simulation's stream.
+    --workload eam profiles the Sutton-Chen copper system instead of the LJ liquid."""
+    if args.workload == "eam":
+        sim, natoms = make_eam_sim(args.precision)
+        sim.set_option("graph_mode", 0)
+        sim.update_forces()
+        sim.do_steps(args.melt + args.warmup)
+        sim.do_steps(args.steps)
+        sim.synchronize()
+        print(json.dumps({"profile": True, "workload": "eam", "natoms": natoms, "steps": args.steps, **sim.stats()}))
+        return
     w = workload()
     sim = make_sim(w, args.precision)
     sim.set_option("graph_mode", 0)
@@ -595,29 +606,39 @@ def served_stream(device: int, njobs: int, rate: float, rank: int = 0, world: in
     return out
 
 
+def make_eam_sim(precision: str, device: int = 0, state: dict | None = None, ncell: int = 50):
+    """Sutton-Chen copper, FCC ncell^3 at a = 3.61 A minus 1 % of the sites, 300 K (or `state`),
+    linkedcell with cells of edge 2a = cutoff, velocityverlet dt 2 fs."""
+    from lpmd2_gb300 import gbmd
+    from lpmd2_gb300 import inputs as I
+
+    w = I.sc_cu_system(ncell, seed=3)
+    state = state or w
+    c = I.SC_CU
+    nx = int(round(w["L"][0] / (2 * c["a"])))
+    sim = gbmd.Simulation(w["natoms"], w["L"], device=device)
+    sim.set_atoms(state["pos"], state["vel"], Z=w["Z"], mass=w["mass"])
+    sim.set_cell_manager(gbmd.Plugin("linkedcell", f"cutoff {2 * c['a']!r} nx {nx} ny {nx} nz {nx}"))
+    sim.add_potential(gbmd.Plugin("suttonchen", f"e {c['e']} a {c['a']} n {c['n']} m {c['m']} c {c['c']} "
+                                                f"cutoff {2 * c['a']!r}"))
+    sim.set_integrator(gbmd.Plugin("velocityverlet", "dt 2.0"))
+    sim.set_precision(precision)
+    sim.set_option("graph_block", GRAPH_BLOCK)
+    return sim, w["natoms"]
+
+
 def eam_metal(device: int, steps: int, ncell: int = 50) -> dict:
     """Sutton-Chen copper: FCC 50^3 at a = 3.61 A with 1 % of the sites removed (495,000 atoms),
     300 K, linkedcell nx 25 (cell edge = cutoff = 7.22 A), velocityverlet dt 2 fs.  Mixed and
     FP64 throughput, and the mixed path's force RMS, energy and virial-pressure errors against
     FP64 at the same state."""
-    from lpmd2_gb300 import gbmd
     from lpmd2_gb300 import inputs as I
 
     w = I.sc_cu_system(ncell, seed=3)
-    c = I.SC_CU
     N = w["natoms"]
-    nx = int(round(w["L"][0] / (2 * c["a"])))
 
     def make(prec, state):
-        sim = gbmd.Simulation(N, w["L"], device=device)
-        sim.set_atoms(state["pos"], state["vel"], Z=w["Z"], mass=w["mass"])
-        sim.set_cell_manager(gbmd.Plugin("linkedcell", f"cutoff {2 * c['a']!r} nx {nx} ny {nx} nz {nx}"))
-        sim.add_potential(gbmd.Plugin("suttonchen", f"e {c['e']} a {c['a']} n {c['n']} m {c['m']} c {c['c']} "
-                                                    f"cutoff {2 * c['a']!r}"))
-        sim.set_integrator(gbmd.Plugin("velocityverlet", "dt 2.0"))
-        sim.set_precision(prec)
-        sim.set_option("graph_block", GRAPH_BLOCK)
-        return sim
+        return make_eam_sim(prec, device, state, ncell)[0]
 
     # time the mixed path from the lattice; its final (thermalised) state is where the
     # errors are measured: on the perfect lattice the forces nearly cancel

@@ -775,8 +775,10 @@ struct Engine::Impl {
       const int mode = sysd[0].mode;
       if (P.kind != POT_LJ) {
         int first = (p == first_eam);
-        if (mixed)
-          k_eam_density<NB_LIST, 1><<<ntiles, TILE, 0, s>>>(D, P, first);
+        if (mixed && P.kind == POT_SC && P.int_m == 6)
+          k_eam_density32<6><<<ntiles, TILE, 0, s>>>(D, P);
+        else if (mixed)
+          k_eam_density32<0><<<ntiles, TILE, 0, s>>>(D, P);
         else if (mode == NB_LIST)
           k_eam_density<NB_LIST, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
         else if (mode == NB_CELLS)
@@ -793,8 +795,15 @@ struct Engine::Impl {
           else
             k_force32<PC_PAIR, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
         } else {
+          // Sutton-Chen exponent pairs of common metals get straight-line powers
+          const bool sc96 = P.kind == POT_SC && P.int_n == 9 && P.int_m == 6;
+          const bool sc126 = P.kind == POT_SC && P.int_n == 12 && P.int_m == 6;
           if (species)
             k_force32<PC_EAM, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
+          else if (sc96)
+            k_force32<PC_EAM, 0, 9, 6><<<ntiles, TILE, 0, s>>>(D, P, sp);
+          else if (sc126)
+            k_force32<PC_EAM, 0, 12, 6><<<ntiles, TILE, 0, s>>>(D, P, sp);
           else
             k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
         }

@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_
 #define GBMD_FORCE_MIN_BLOCKS 8
 #endif
 
-template <int PC, int SPECIES>
+template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
 __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
   __shared__ float4 shifts[125];
   const int tile = blockIdx.x;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       if (PC == PC_PAIR) {
         lj_pair32(P, rcp_approx(r2), g, en);
       } else {
-        eam_pair32(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
+        eam_pair32_t<SCN, SCM>(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
       }
       g = in ? g : 0.0f;
       ep += in ? en : 0.0f;
@@ -463,6 +463,66 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
 // ------------------------------------------------------------------------------------------
 // EAM density pass + embedding (FP64 embedding in both precisions).
 // ------------------------------------------------------------------------------------------
+
+// Mixed density pass over the Verlet list: FP32 rho_ij of each group of four entries
+// (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
+// density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
+template <int SCM>
+__global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
+  __shared__ float4 shifts[125];
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
+  const SysDev& S = D.sysd[s];
+  if (!S.active) return;  // whole block: one tile belongs to one system
+  load_shifts(S, shifts);
+  const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;
+  const long long i = S.atom_base + li;
+  const bool active = (int)threadIdx.x < D.tile_count[tile];
+  double F = 0.0;
+  if (active) {
+    const float4* __restrict__ g32 = D.g32 + S.atom_base;
+    const float4 gi = g32[li];
+    const float rc2_lo = P.f[12], rc2_hi = P.f[13];
+    const int na = S.natoms;
+    const int cnt = D.ncount[i];
+    const uint4* L = list_group(D, S, li, 0);
+    Fix q;
+    unsigned rechecks = 0;
+    auto term = [&](unsigned e, bool valid) -> float {
+      const int j = (int)(e & LOCAL_MASK);
+      const float4 gj = g32[j];
+      const float4 sh = shifts[e >> CODE_SHIFT];
+      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      bool in = valid && r2 < rc2_lo;
+      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
+        in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
+        ++rechecks;
+      }
+      const float v = eam_rho32_t<SCM>(P, r2);
+      return in ? v : 0.0f;
+    };
+    const float scale = (float)FIX_RHO;
+    for (int g = 0; g < (cnt + 3) >> 2; ++g) {
+      const uint4 e4 = __ldg(L + (long long)g * na);
+      const int rem = cnt - 4 * g;
+      const float part = ((term(e4.x, true) + term(e4.y, rem > 1)) + term(e4.z, rem > 2)) + term(e4.w, rem > 3);
+      q.add(part * scale);
+    }
+    if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
+    const double rho = (double)q.value() * (1.0 / FIX_RHO);
+    double phi;
+    eam_embed64(P, rho, F, phi);
+    D.rho[i] = rho;
+    D.phi[i] = phi;
+    D.phif[i] = (float)phi;
+  }
+  // FP64 embedding energies summed exactly as int64 fixed point (2^-32 eV per atom)
+  long long v[1] = {active ? __double2ll_rn(F * FIX_E) : 0ll};
+  long long t[1];
+  block_sum<long long, 1>(v, t);
+  if (threadIdx.x == 0) atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_EEMBED, (unsigned long long)t[0]);
+}
 
 template <int NB, int MIXED>
 __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int first) {

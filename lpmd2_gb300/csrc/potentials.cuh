@@ -178,6 +178,20 @@ __device__ __forceinline__ float eam_rho32(const PotParams& P, float r2) {
   }
 }
 
+// x^N for a compile-time N by repeated squaring (straight-line code).
+template <int N>
+__device__ __forceinline__ float ipow_c(float x) {
+  if constexpr (N == 0) {
+    return 1.0f;
+  } else if constexpr (N == 1) {
+    return x;
+  } else if constexpr (N % 2 == 0) {
+    const float h = ipow_c<N / 2>(x);
+    return h * h;
+  } else {
+    return x * ipow_c<N - 1>(x);
+  }
+}
 // s with F_i = s * r_ij (note: r_ij, not r^) and pair energy e.
 __device__ __forceinline__ void eam_pair32(const PotParams& P, float r2, float phi_i, float phi_j, float& s,
                                            float& e) {
@@ -215,6 +229,34 @@ __device__ __forceinline__ void eam_pair32(const PotParams& P, float r2, float p
       mb = -t1 * t2;
     }
     s = (pf + mb) * ir;
+  }
+}
+
+// Sutton-Chen with the exponents n = N, m = M known at compile time (the kernels are
+// instantiated for the common pairs); N = M = 0 selects the run-time forms above.
+template <int M>
+__device__ __forceinline__ float eam_rho32_t(const PotParams& P, float r2) {
+  if constexpr (M > 0) {
+    if constexpr (M % 2 == 0)
+      return P.f[3] * ipow_c<M / 2>(rcp_approx(r2));
+    else
+      return P.f[3] * ipow_c<M>(rsqrtf(r2));
+  } else {
+    return eam_rho32(P, r2);
+  }
+}
+
+template <int N, int M>
+__device__ __forceinline__ void eam_pair32_t(const PotParams& P, float r2, float phi_i, float phi_j, float& s,
+                                             float& e) {
+  if constexpr (N > 0) {
+    const float ir = rsqrtf(r2);
+    const float irm1 = ipow_c<M + 1>(ir);
+    const float irn = ipow_c<N>(ir);
+    e = P.f[0] * irn;
+    s = (P.f[1] * irn * ir + P.f[2] * (phi_i + phi_j) * irm1) * ir;
+  } else {
+    eam_pair32(P, r2, phi_i, phi_j, s, e);
   }
 }
 

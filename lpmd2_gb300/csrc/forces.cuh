@@ -464,12 +464,51 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
 // EAM density pass + embedding (FP64 embedding in both precisions).
 // ------------------------------------------------------------------------------------------
 
+// Streams the list groups of the calling warp's 32 atoms (32 x 16 bytes, contiguous for a
+// fixed group index) through the warp's RING-stage shared-memory ring with bulk asynchronous
+// copies, calling body(group q, this lane's uint4 of that group) for q < ngw, the warp's
+// largest group count.  Lane 0 issues the copies; every wait is bounded.  Returns false if a
+// wait gave up.
+template <class F>
+__device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
+                                               uint4 (*ring)[32], unsigned long long* bar, F&& body) {
+  const int lane = threadIdx.x & 31;
+  const uint4* src0 = list_group(D, S, wfirst, 0);
+  const unsigned bytes = (unsigned)wcount * 16u;
+  const int na = S.natoms;
+  if (lane == 0 && ngw > 0) {
+    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
+    mbar_init_fence();
+    for (int r = 0; r < RING && r < ngw; ++r) {
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
+    }
+  }
+  __syncwarp();
+  bool waited = true;
+  for (int q = 0; q < ngw; ++q) {
+    const int r = q & (RING - 1);
+    if (!mbar_wait_bounded(&bar[r], (unsigned)((q / RING) & 1))) waited = false;
+    const uint4 cur = ring[r][lane];
+    __syncwarp();  // every lane has its entry: the stage can be refilled
+    if (lane == 0 && q + RING < ngw) {
+      fence_proxy_async_shared();
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)(q + RING) * na, bytes, &bar[r]);
+    }
+    body(q, cur);
+  }
+  return waited;
+}
+
 // Mixed density pass over the Verlet list: FP32 rho_ij of each group of four entries
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
 template <int SCM>
 __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   __shared__ float4 shifts[125];
+  __shared__ __align__(16) uint4 ring_s[TILE / 32][RING][32];
+  __shared__ __align__(8) unsigned long long bar_s[TILE / 32][RING];
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
@@ -478,38 +517,44 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;
   const long long i = S.atom_base + li;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
-  double F = 0.0;
-  if (active) {
-    const float4* __restrict__ g32 = D.g32 + S.atom_base;
-    const float4 gi = g32[li];
-    const float rc2_lo = P.f[12], rc2_hi = P.f[13];
-    const int na = S.natoms;
-    const int cnt = D.ncount[i];
-    const uint4* L = list_group(D, S, li, 0);
-    Fix q;
-    unsigned rechecks = 0;
-    auto term = [&](unsigned e, bool valid) -> float {
-      const int j = (int)(e & LOCAL_MASK);
-      const float4 gj = g32[j];
-      const float4 sh = shifts[e >> CODE_SHIFT];
-      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      bool in = valid && r2 < rc2_lo;
-      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
-        in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
-        ++rechecks;
-      }
-      const float v = eam_rho32_t<SCM>(P, r2);
-      return in ? v : 0.0f;
-    };
-    const float scale = (float)FIX_RHO;
-    for (int g = 0; g < (cnt + 3) >> 2; ++g) {
-      const uint4 e4 = __ldg(L + (long long)g * na);
+  const float4* __restrict__ g32 = D.g32 + S.atom_base;
+  const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float rc2_lo = P.f[12], rc2_hi = P.f[13];
+  const int cnt = active ? D.ncount[i] : 0;
+  const int ng = (cnt + 3) >> 2;
+  Fix q;
+  unsigned rechecks = 0;
+  auto term = [&](unsigned e, bool valid) -> float {
+    const int j = (int)(e & LOCAL_MASK);
+    const float4 gj = g32[j];
+    const float4 sh = shifts[e >> CODE_SHIFT];
+    const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    bool in = valid && r2 < rc2_lo;
+    if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
+      in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
+      ++rechecks;
+    }
+    const float v = eam_rho32_t<SCM>(P, r2);
+    return in ? v : 0.0f;
+  };
+  const float scale = (float)FIX_RHO;
+  // every lane of the warp takes part in the ring (lanes without an atom have no groups)
+  const int w = threadIdx.x >> 5;
+  const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
+  const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
+  const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
+  const bool waited = warp_list_ring(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], [&](int g, const uint4& e4) {
+    if (g < ng) {
       const int rem = cnt - 4 * g;
       const float part = ((term(e4.x, true) + term(e4.y, rem > 1)) + term(e4.z, rem > 2)) + term(e4.w, rem > 3);
       q.add(part * scale);
     }
-    if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
+  });
+  if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
+  if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
+  double F = 0.0;
+  if (active) {
     const double rho = (double)q.value() * (1.0 / FIX_RHO);
     double phi;
     eam_embed64(P, rho, F, phi);

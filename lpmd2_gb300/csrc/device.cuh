@@ -23,7 +23,6 @@ namespace gbmd {
 constexpr int TILE = 128;          // atoms per tile = threads per block of the per-atom kernels
 constexpr int THERMO_LEN = 22;
 constexpr int PART_D = 16;         // FP64 per-tile partial sums
-constexpr int PART_I = 12;         // int64 fixed-point per-tile partial sums (mixed path)
 constexpr int CODE_SHIFT = 25;
 constexpr unsigned LOCAL_MASK = (1u << CODE_SHIFT) - 1u;
 constexpr int MAX_SYSTEM_ATOMS = (1 << CODE_SHIFT);
@@ -45,8 +44,6 @@ constexpr int RING = 4;            // shared-memory stages of the list ring in t
 
 // Per-tile partial-sum slots (FP64)
 enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX = 13 };
-// Per-tile partial-sum slots (int64, mixed path)
-enum { PI_EPAIR = 0, PI_VIR = 1, PI_STRESS = 2 };
 // Per-system int64 fixed-point accumulators of the mixed path (atomics from every block)
 enum { SA_EPAIR = 0, SA_VIR = 1, SA_STRESS = 2, SA_KE = 11, SA_P = 12, SA_EEMBED = 15, SA_LEN = 16 };
 constexpr double FIX_KE = 17592186044416.0;  // 2^44: kinetic energy (amu A^2/fs^2) and momentum
@@ -128,7 +125,6 @@ struct Dev {
   double* dacc;      // 3*N FP64
   // reductions
   double* tile_d;
-  long long* tile_i;
   unsigned long long* sys_acc;  // nsys * SA_LEN
   const SysDev* sysd;
   SysState* sst;

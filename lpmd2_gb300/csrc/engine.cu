@@ -481,7 +481,6 @@ struct Engine::Impl {
     D.facc = alloc<long long>(3 * n);
     D.dacc = alloc<double>(3 * n);
     D.tile_d = alloc<double>((size_t)ntiles * PART_D);
-    D.tile_i = alloc<long long>((size_t)ntiles * PART_I);
     D.sys_acc = alloc<unsigned long long>((size_t)nsys * SA_LEN);
     D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
     D.log_cap = log_cap;
@@ -780,11 +779,11 @@ struct Engine::Impl {
         else if (mixed)
           k_eam_density32<0><<<ntiles, TILE, 0, s>>>(D, P);
         else if (mode == NB_LIST)
-          k_eam_density<NB_LIST, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+          k_eam_density<NB_LIST><<<ntiles, TILE, 0, s>>>(D, P, first);
         else if (mode == NB_CELLS)
-          k_eam_density<NB_CELLS, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+          k_eam_density<NB_CELLS><<<ntiles, TILE, 0, s>>>(D, P, first);
         else
-          k_eam_density<NB_ALLPAIRS, 0><<<ntiles, TILE, 0, s>>>(D, P, first);
+          k_eam_density<NB_ALLPAIRS><<<ntiles, TILE, 0, s>>>(D, P, first);
         launched();
       }
       if (mixed) {
@@ -829,7 +828,7 @@ struct Engine::Impl {
     if (mixed)
       k_tail<<<1, 256, 0, s>>>(D, count_step, decide_next, (unsigned long long)cond_next);
     else
-      k_thermo<<<nsys, TILE, 0, s>>>(D, 0, count_step);
+      k_thermo<<<nsys, TILE, 0, s>>>(D, count_step);
     launched();
   }
 

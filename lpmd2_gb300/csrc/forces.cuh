@@ -569,89 +569,60 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   if (threadIdx.x == 0) atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_EEMBED, (unsigned long long)t[0]);
 }
 
-template <int NB, int MIXED>
+// FP64 density pass (the plain path, any neighbour mode): reference r and rhoij, FP64
+// embedding, per-tile FP64 partial of the embedding energy.
+template <int NB>
 __global__ void __launch_bounds__(TILE) k_eam_density(Dev D, PotParams P, int first) {
-  __shared__ float4 shifts[125];
   const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   if (!S.active) return;  // whole block: one tile belongs to one system
-  if (MIXED) load_shifts(S, shifts);
   const long long i = D.tile_first[tile] + threadIdx.x;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
   double F = 0.0;
   if (active) {
     double rho = 0.0;
-    if (MIXED) {
-      Fix q;
-      const float4 gi = D.g32[i];
-      const float rc2_lo = P.f[12], rc2_hi = P.f[13];
-      const float scale = (float)FIX_RHO;
-      for_each_candidate<NB_LIST>(D, S, i, [&](long long j, unsigned code) {
-        const float4 gj = D.g32[j];
-        const float4 sh = shifts[code];
-        float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-        float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2_hi) {
-          bool in = r2 < rc2_lo;
-          if (!in) in = exact_inside(D, S, i, j, P.rc2);
-          if (in) q.add(eam_rho32(P, r2) * scale);
-        }
-      });
-      rho = (double)q.value() * (1.0 / FIX_RHO);
-    } else {
-      const double4_32a pi = D.g64[i];
-      for_each_candidate<NB>(D, S, i, [&](long long j, unsigned) {
-        const double4_32a pj = D.g64[j];
-        double dx = ref_wrap(dsub(pj.x, pi.x), S.L[0], S.Lh[0]);
-        double dy = ref_wrap(dsub(pj.y, pi.y), S.L[1], S.Lh[1]);
-        double dz = ref_wrap(dsub(pj.z, pi.z), S.L[2], S.Lh[2]);
-        double r2 = ref_sq(dx, dy, dz);
-        if (r2 < P.rc2) rho += eam_rho64(P, sqrt(r2));
-      });
-    }
+    const double4_32a pi = D.g64[i];
+    for_each_candidate<NB>(D, S, i, [&](long long j, unsigned) {
+      const double4_32a pj = D.g64[j];
+      double dx = ref_wrap(dsub(pj.x, pi.x), S.L[0], S.Lh[0]);
+      double dy = ref_wrap(dsub(pj.y, pi.y), S.L[1], S.Lh[1]);
+      double dz = ref_wrap(dsub(pj.z, pi.z), S.L[2], S.Lh[2]);
+      double r2 = ref_sq(dx, dy, dz);
+      if (r2 < P.rc2) rho += eam_rho64(P, sqrt(r2));
+    });
     double phi;
     eam_embed64(P, rho, F, phi);
     D.rho[i] = rho;
     D.phi[i] = phi;
     D.phif[i] = (float)phi;
   }
-  if (MIXED) {
-    // FP64 embedding energies summed exactly as int64 fixed point (2^-32 eV per atom)
-    long long v[1] = {active ? __double2ll_rn(F * FIX_E) : 0ll};
-    long long t[1];
-    block_sum<long long, 1>(v, t);
-    if (threadIdx.x == 0) atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_EEMBED, (unsigned long long)t[0]);
-  } else {
-    double v[1] = {F};
-    double t[1];
-    block_sum<double, 1>(v, t);
-    if (threadIdx.x == 0) {
-      double* td = D.tile_d + (long long)tile * PART_D;
-      td[PD_EEMBED] = first ? t[0] : td[PD_EEMBED] + t[0];
-    }
+  double v[1] = {F};
+  double t[1];
+  block_sum<double, 1>(v, t);
+  if (threadIdx.x == 0) {
+    double* td = D.tile_d + (long long)tile * PART_D;
+    td[PD_EEMBED] = first ? t[0] : td[PD_EEMBED] + t[0];
   }
 }
 
 // ------------------------------------------------------------------------------------------
-// Thermo record per system (one block per system; fixed-order reductions).
+// Thermo record per system of the FP64 path (one block per system; fixed-order tile sums).
 // ------------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(TILE) k_thermo(Dev D, int mixed, int count_step) {
+__global__ void __launch_bounds__(TILE) k_thermo(Dev D, int count_step) {
   const int s = blockIdx.x;
   const SysDev& S = D.sysd[s];
   if (!S.active) return;
   double v[PART_D];
   for (int k = 0; k < PART_D; ++k) v[k] = 0.0;
-  if (!mixed) {
-    for (int t = threadIdx.x; t < S.ntiles; t += blockDim.x) {
-      const double* td = D.tile_d + (long long)(S.tile_base + t) * PART_D;
-      for (int k = 0; k < PART_D; ++k) v[k] += td[k];
-    }
+  for (int t = threadIdx.x; t < S.ntiles; t += blockDim.x) {
+    const double* td = D.tile_d + (long long)(S.tile_base + t) * PART_D;
+    for (int k = 0; k < PART_D; ++k) v[k] += td[k];
   }
   double tot[PART_D];
-  if (!mixed) block_sum<double, PART_D>(v, tot);  // block-uniform branch
-  if (threadIdx.x == 0) thermo_record(D, s, mixed ? nullptr : tot, count_step);
+  block_sum<double, PART_D>(v, tot);
+  if (threadIdx.x == 0) thermo_record(D, s, tot, count_step);
 }
 
 }  // namespace gbmd

@@ -174,10 +174,10 @@ __global__ void k_scatter(Dev D) {
   D.perm[p] = (int)i;
 }
 
-// One warp per cell (grid.y = system): orders the cell's slots by original index, the order in
-// which LinkedCell's head/next lists visit them.  Up to 32 atoms: each lane ranks its atom by
-// counting smaller tags across the warp; larger cells fall back to an insertion sort by lane 0.
-// One warp per cell over the cells of every system (flat index g; cell_sys maps it back).
+// One warp per cell over the cells of every system (flat index g; cell_sys maps it back):
+// orders the cell's slots by original index, the order in which LinkedCell's head/next lists
+// visit them.  Up to 32 atoms: each lane ranks its atom by counting smaller tags across the
+// warp; larger cells fall back to an insertion sort by lane 0.
 __global__ void k_cellsort(Dev D) {
   const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (g >= D.total_cells) return;
@@ -315,10 +315,11 @@ __global__ void k_copyback(Dev D) {
 
 __device__ __forceinline__ int shift_code(int kx, int ky, int kz) { return (kx + 2) + 5 * ((ky + 2) + 5 * (kz + 2)); }
 
-// One warp per home cell (grid.y = system): the lanes hold up to 32 atoms of the cell, and the
-// atoms of each stencil cell are staged through shared memory 32 at a time; every lane then
-// tests the staged candidate against its own atom (broadcast reads, no divergence between
-// lanes, since all atoms of a cell share the stencil and its cell-shift codes).
+// One warp per home cell (per-block table of system and cells): the lanes hold up to 32 atoms
+// of the cell, and the atoms of each stencil cell are staged through shared memory 32 at a
+// time; every lane then tests the staged candidate against its own atom (broadcast reads, no
+// divergence between lanes, since all atoms of a cell share the stencil and its cell-shift
+// codes), and appends its hits in candidate order through a bit mask.
 constexpr int LIST_WARPS = 4;
 // Resident blocks per SM the register allocation of the list build is sized for.
 #ifndef GBMD_LIST_MIN_BLOCKS

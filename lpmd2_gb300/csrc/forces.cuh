@@ -329,6 +329,11 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     const int na = S.natoms;
     const int cnt = active ? D.ncount[i] : 0;
     const int ng = (cnt + 3) >> 2;
+    // Guard-band entries (a few per thousand atoms) are only noted in the loop and decided in
+    // FP64 afterwards; their forces then go straight into the fixed-point sums.
+    constexpr unsigned NO_BAND = 0xffffffffu;
+    unsigned band_e = NO_BAND;
+    bool band_more = false;
     // Branch-free body: every candidate is evaluated and out-of-range pairs are masked to
     // zero, so lanes never diverge on the cutoff test (70% of Verlet-list entries are inside).
     // Returns g with f = g * d; the caller sums a group's four forces in FP32 and adds the
@@ -342,9 +347,11 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       dz = (sh.z + gj.z) - gi.z;
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       bool in = valid && r2 < rc2_lo;
-      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // inside the guard band: decide in FP64 like the reference
-        in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
-        ++rechecks;
+      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // guard band: decided in FP64 after the loop
+        if (band_e == NO_BAND)
+          band_e = e;
+        else
+          band_more = true;
       }
       if (SPECIES) in = in && applies_to(P.spc_sum, ti, __float_as_int(gj.w));
       float g, en;
@@ -409,6 +416,52 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       }
     }
     if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
+    if (band_e != NO_BAND) {
+      // exact FP64 cutoff decision (the reference's Displacement and r^2) for the guard-band
+      // entries; one noted entry per atom, else a rescan of the atom's list
+      auto settle = [&](unsigned e) {
+        const int j = (int)(e & LOCAL_MASK);
+        const float4 gj = g32[j];
+        const float4 sh = shifts[e >> CODE_SHIFT];
+        const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
+        ++rechecks;
+        if (!exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) return;
+        if (SPECIES && !applies_to(P.spc_sum, ti, __float_as_int(gj.w))) return;
+        float g, en;
+        if (PC == PC_PAIR) {
+          lj_pair32(P, rcp_approx(r2), g, en);
+        } else {
+          eam_pair32_t<SCN, SCM>(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
+        }
+        const float fx = g * dx, fy = g * dy, fz = g * dz;
+        fqx.add_scaled32(fx);
+        fqy.add_scaled32(fy);
+        fqz.add_scaled32(fz);
+        bad |= fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) > 4000.0f;
+        ep += en;
+        sxx = fmaf(fx, dx, sxx);
+        sxy = fmaf(fx, dy, sxy);
+        sxz = fmaf(fx, dz, sxz);
+        syy = fmaf(fy, dy, syy);
+        syz = fmaf(fy, dz, syz);
+        szz = fmaf(fz, dz, szz);
+      };
+      if (!band_more) {
+        settle(band_e);
+      } else {
+        const uint4* L = list_group(D, S, li, 0);
+        for (int q = 0; q < ng; ++q) {
+          const uint4 e4 = __ldg(L + (long long)q * na);
+          const int rem = cnt - 4 * q;
+          settle(e4.x);
+          if (rem > 1) settle(e4.y);
+          if (rem > 2) settle(e4.z);
+          if (rem > 3) settle(e4.w);
+        }
+      }
+    }
   }
   double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
   float d2 = 0.0f;
@@ -524,16 +577,22 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   const int ng = (cnt + 3) >> 2;
   Fix q;
   unsigned rechecks = 0;
+  // guard-band entries are noted in the loop and decided in FP64 afterwards (as in k_force32)
+  constexpr unsigned NO_BAND = 0xffffffffu;
+  unsigned band_e = NO_BAND;
+  bool band_more = false;
   auto term = [&](unsigned e, bool valid) -> float {
     const int j = (int)(e & LOCAL_MASK);
     const float4 gj = g32[j];
     const float4 sh = shifts[e >> CODE_SHIFT];
     const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    bool in = valid && r2 < rc2_lo;
+    const bool in = valid && r2 < rc2_lo;
     if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
-      in = exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2);
-      ++rechecks;
+      if (band_e == NO_BAND)
+        band_e = e;
+      else
+        band_more = true;
     }
     const float v = eam_rho32_t<SCM>(P, r2);
     return in ? v : 0.0f;
@@ -552,6 +611,31 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
     }
   });
   if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
+  if (band_e != NO_BAND) {
+    auto settle = [&](unsigned e) {
+      const int j = (int)(e & LOCAL_MASK);
+      const float4 gj = g32[j];
+      const float4 sh = shifts[e >> CODE_SHIFT];
+      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
+      ++rechecks;
+      if (exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) q.add(eam_rho32_t<SCM>(P, r2) * scale);
+    };
+    if (!band_more) {
+      settle(band_e);
+    } else {
+      const uint4* L = list_group(D, S, li, 0);
+      for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = __ldg(L + (long long)g * S.natoms);
+        const int rem = cnt - 4 * g;
+        settle(e4.x);
+        if (rem > 1) settle(e4.y);
+        if (rem > 2) settle(e4.z);
+        if (rem > 3) settle(e4.w);
+      }
+    }
+  }
   if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
   double F = 0.0;
   if (active) {

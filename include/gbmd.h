@@ -195,6 +195,21 @@ gbmd_status gbmd_sim_stats(gbmd_sim* sim, gbmd_stats* out);
 /* The cudaStream_t the simulation's kernels run on. */
 gbmd_status gbmd_sim_stream(gbmd_sim* sim, void** stream);
 
+/* Thermostats applied between steps (LPMD's modifiers, which run after DoStep).  The
+ * temperature is measured from the current velocities, as the modifiers measure it; the thermo
+ * record of the step stays as the step reported it (LPMD's monitor prints those tags):
+ *   GBMD_SCALE_SET_TEMPERATURE  T over the atoms without fixedvel/fixedpos, v *= sqrt(target / T)
+ *       for those atoms: SimulationBuilder::SetTemperature
+ *       (liblpmd/simulation/simulationbuilder.cc:53-72), used by the tempscaling and temperature
+ *       modifiers (plugins/tempscaling.cc:66-71, plugins/temperature.cc:58-62)
+ *   GBMD_SCALE_BERENDSEN        T over all atoms, v *= sqrt(1 + dt_over_tau * (target / T - 1))
+ *       for every atom: BerendsenModifier::Apply (plugins/berendsen.cc:72-99)
+ * A system at T = 0 is left unchanged.  The next step's position update is redone with the new
+ * velocities. */
+#define GBMD_SCALE_SET_TEMPERATURE 0
+#define GBMD_SCALE_BERENDSEN 1
+gbmd_status gbmd_sim_scale_velocities(gbmd_sim* sim, int mode, double target, double dt_over_tau);
+
 /* Checkpoint / restore, replacing Simulation::Dump / Restore
  * (liblpmd/simulation/simulationbuilder.cc:195-293), which write 6-significant-digit text:
  * a binary snapshot of the complete state (atoms in device order, lists, counters, thermo
@@ -247,6 +262,8 @@ gbmd_status gbmd_batch_synchronize(gbmd_batch* batch);
 gbmd_status gbmd_batch_thermo(gbmd_batch* batch, int sys, gbmd_thermo* out);
 gbmd_status gbmd_batch_stats(gbmd_batch* batch, gbmd_stats* out);
 gbmd_status gbmd_batch_stream(gbmd_batch* batch, void** stream);
+/* gbmd_sim_scale_velocities for system `sys` of a batch (-1: every active system). */
+gbmd_status gbmd_batch_scale_velocities(gbmd_batch* batch, int sys, int mode, double target, double dt_over_tau);
 /* gbmd_sim_checkpoint_* for a whole batch. */
 gbmd_status gbmd_batch_checkpoint_size(gbmd_batch* batch, size_t* bytes);
 gbmd_status gbmd_batch_checkpoint_save(gbmd_batch* batch, void* buf, size_t bytes);

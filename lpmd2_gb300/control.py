@@ -14,13 +14,16 @@ simulation it describes through libgbmd:
   cellmanager <id> / potential <id> A B / integrator <id>      wiring (ids of use blocks)
   steps N                                                      velocity-Verlet steps
   monitor p1,p2,... [start= end= each= output=]                thermo columns (monitor.cc)
+  use tempscaling|temperature|berendsen ... enduse; apply <id>  thermostats between steps
   output xyz <file> [each= start= end= level=]                 XYZ frames (xyz.cc)
   mass <symbol> <value>, set <option> <value>, periodic x y z
 
 Thermo comes from the device's per-step record, so monitored steps cost no extra
-synchronisation; positions are copied back only for the output frames.  Statements of
-modules outside the timestep (property, apply, visualize, filter, average, other plugins'
-use blocks) are reported and skipped, or rejected with --strict.
+synchronisation; positions are copied back only for the output frames.  Thermostats
+(tempscaling, temperature, berendsen) rescale velocities on the device between steps, on the
+schedule of their `apply` statements.  Statements of modules outside the timestep (property,
+visualize, filter, average, other plugins' use blocks and applies) are reported and skipped,
+or rejected with --strict.
 
 `prepare temperature` draws seeded Maxwell-Boltzmann velocities with zero total momentum,
 rescaled to exactly T (seed 1 unless `seed=` is given): the reference's modifier is seeded from
@@ -41,7 +44,8 @@ from . import inputs as I
 
 TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "finnissinclair",
                     "finnissinclair-ext", "velocityverlet"}
-SKIPPED_STATEMENTS = {"property", "apply", "visualize", "filter", "average", "bond", "charge", "plugindir"}
+MODIFIER_PLUGINS = {"tempscaling", "temperature", "berendsen"}
+SKIPPED_STATEMENTS = {"property", "visualize", "filter", "average", "bond", "charge", "plugindir"}
 
 # Element symbols in order of atomic number (the periodic table up to Rn).
 _SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
@@ -67,6 +71,8 @@ class Control:
     outputs: list[dict] = dataclasses.field(default_factory=list)
     monitors: list[dict] = dataclasses.field(default_factory=list)
     uses: dict[str, tuple[str, str]] = dataclasses.field(default_factory=dict)  # id -> (plugin, args)
+    modifiers: dict[str, tuple[str, str]] = dataclasses.field(default_factory=dict)  # id -> (plugin, args)
+    applies: list[tuple[str, dict]] = dataclasses.field(default_factory=list)  # (id, statement args)
     cellmanager: str | None = None
     potentials: list[tuple[str, str, str]] = dataclasses.field(default_factory=list)
     integrator: str | None = None
@@ -124,6 +130,8 @@ def parse(text: str, strict: bool = False) -> Control:
             i += 1
             if plugin in TIMESTEP_PLUGINS:
                 ctl.uses[uid] = (plugin, " ".join(body))
+            elif plugin in MODIFIER_PLUGINS:
+                ctl.modifiers[uid] = (plugin, " ".join(body))
             else:
                 ctl.skipped.append(f"use {plugin}")
             continue
@@ -138,6 +146,8 @@ def parse(text: str, strict: bool = False) -> Control:
                 ctl.cell = np.array([L, L, L])
             elif kind == "crystal":
                 a = _args(rest[1:], ["a", "b", "c", "alpha", "beta", "gamma", "scale"])
+                if "b" not in a:  # a crystal cell given by `a` alone is cubic (lpmd/controlparser.cc:81-87)
+                    a["b"] = a["c"] = a["a"]
                 if any(abs(float(a.get(k, 90.0)) - 90.0) > 1e-12 for k in ("alpha", "beta", "gamma")):
                     raise ControlError("only orthogonal cells run on the GPU path")
                 sc = float(a.get("scale", 1.0))
@@ -168,6 +178,12 @@ def parse(text: str, strict: bool = False) -> Control:
             ctl.options[rest[0]] = rest[1] if len(rest) > 1 else ""
         elif name == "periodic":
             ctl.periodic = tuple(_true(x) for x in rest[:3])
+        elif name == "apply":
+            a = _args(rest, ["module"]) if "over" not in rest else {}
+            if a.get("module") in ctl.modifiers:
+                ctl.applies.append((a.pop("module"), a))
+            else:
+                ctl.skipped.append(ln)
         elif name in SKIPPED_STATEMENTS:
             ctl.skipped.append(ln)
         else:
@@ -209,6 +225,61 @@ def _active(step: int, start: int, end: int, each: int) -> bool:
     if step < start or (end != -1 and step > end):
         return False
     return (step - start) % each == 0
+
+
+def _kv(args: str) -> dict:
+    w = args.split()
+    return {w[k]: w[k + 1] for k in range(0, len(w) - 1, 2)}
+
+
+def modifier_schedule(ctl: Control, dt: float) -> list[tuple[int, int, float, float]]:
+    """The velocity rescalings the applied modifiers make, as (step, mode, target T, dt/tau)
+    after that step, in the order lpmd runs them (Application::RunModifiers after DoStep,
+    lpmd/application.cc:403-464).  Stepper activity and the linear ramp follow
+    liblpmd/lpmd/stepper.h:17-31, with `end` -1 replaced by the step count; tempscaling and
+    temperature call SetTemperature (plugins/tempscaling.cc:66-71, plugins/temperature.cc:35-39);
+    berendsen (plugins/berendsen.cc:72-99) switches itself on at its first active step (no
+    rescaling then), applies every step until tau/dt steps later, and switches off on the
+    step after."""
+    out = []
+    mods = []
+    for uid, extra in ctl.applies:
+        plugin, body = ctl.modifiers[uid]
+        kw = {"start": "0", "end": "-1", "each": "1", "from": "300.0", "to": "300.0", "t": "300.0", "tau": "400.0"}
+        kw.update(_kv(body))
+        kw.update(extra)
+        if int(kw["each"]) == 0:
+            kw.update(start="0", end="-1", each="1")
+        st = dict(plugin=plugin, start=int(kw["start"]), end=int(kw["end"]), each=int(kw["each"]),
+                  frm=float(kw["from"]), to=float(kw["to"]), t=float(kw["t"]), tau=float(kw["tau"]), stop=-1,
+                  old_each=None)
+        if st["end"] == -1:
+            st["end"] = ctl.steps
+        mods.append(st)
+
+    def ramp(m, k):
+        if m["start"] == m["end"]:
+            return m["frm"]
+        return m["frm"] + float(k - m["start"]) / float(m["end"] - m["start"]) * (m["to"] - m["frm"])
+
+    for k in range(1, ctl.steps + 1):
+        for m in mods:
+            if not _active(k, m["start"], m["end"], m["each"]):
+                continue
+            if m["plugin"] == "tempscaling":
+                out.append((k, 0, ramp(m, k), 0.0))
+            elif m["plugin"] == "temperature":
+                out.append((k, 0, m["t"], 0.0))
+            else:  # berendsen
+                if m["stop"] == -1:
+                    m["stop"] = int(float(k) + m["tau"] / dt)
+                    m["old_each"], m["each"] = m["each"], 1
+                elif k <= m["stop"]:
+                    out.append((k, 1, ramp(m, k), dt / m["tau"]))
+                else:
+                    m["stop"] = -1
+                    m["each"] = m["old_each"]
+    return out
 
 
 def _tags(rec: np.ndarray, natoms: int, L: np.ndarray, masses: np.ndarray) -> dict:
@@ -308,17 +379,32 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         for r in data:
             f.write(symbol + " " + " ".join(f"{x:.8f}" for x in r) + "\n")
 
+    dt = float(_kv(ctl.uses[ctl.integrator][1]).get("dt", "1.0"))
+    schedule = modifier_schedule(ctl, dt)
+    by_step: dict[int, list] = {}
+    for st_, mode, target, dtt in schedule:
+        by_step.setdefault(st_, []).append((mode, target, dtt))
     done = 0
     while done < ctl.steps:
-        # run to the next output frame (or a full thermo log), then report the chunk
+        # run to the next output frame, modifier or full thermo log, then report the chunk
         k = min(ctl.steps - done, 1000)
         for f, st, en, ev, lv in outputs:
             for s in range(done + 1, done + k + 1):
                 if _active(s, st, en, ev):
                     k = s - done
                     break
+        nxt = [t for t in by_step if done < t <= done + k]
+        if nxt:
+            k = min(nxt) - done
         sim.do_steps(k)
         done += k
+        # modifiers, then monitor and output (lpmd/lpmd.cc:93-101): a rescaling step's thermo
+        # record already shows the new velocities
+        for mode, target, dtt in by_step.get(done, []):
+            if mode == 0:
+                sim.set_temperature(target)
+            else:
+                sim.berendsen(target, dtt)
         log = sim.thermo_log()
         for rec in log:
             step = int(round(rec[0]))

@@ -571,6 +571,13 @@ gbmd_status gbmd_batch_checkpoint_load(gbmd_batch* batch, const void* buf, size_
   BATCH_GUARD(batch->eng->checkpoint_load(buf, bytes));
 }
 
+gbmd_status gbmd_sim_scale_velocities(gbmd_sim* sim, int mode, double target, double dt_over_tau) {
+  SIM_GUARD(sim->eng->scale_velocities(-1, mode, target, dt_over_tau));
+}
+gbmd_status gbmd_batch_scale_velocities(gbmd_batch* batch, int sys, int mode, double target, double dt_over_tau) {
+  BATCH_GUARD(batch->eng->scale_velocities(sys, mode, target, dt_over_tau));
+}
+
 gbmd_status gbmd_batch_set_active(gbmd_batch* batch, int sys, int active) {
   BATCH_GUARD(batch->eng->set_active(sys, active != 0));
 }

@@ -1103,6 +1103,24 @@ int wait_selftest(int device, long long polls) {
   return h;
 }
 
+void Engine::scale_velocities(int sys, int mode, double target, double dt_over_tau) {
+  Impl& I = *d_;
+  if (sys >= I.nsys) throw Error(1, "system index out of range");
+  if (mode != 0 && mode != 1) throw Error(1, "velocity scaling mode must be 0 (set temperature) or 1 (Berendsen)");
+  if (!(target >= 0.0)) throw Error(1, "target temperature must be non-negative");
+  if (!I.forces_valid) throw Error(4, "MissingComponent: no evaluated state yet (call update_forces or do_steps first)");
+  CK(cudaSetDevice(I.device));
+  I.set_buffers(I.cbuf);
+  k_kinetic_clear<<<1, 256, 0, I.stream>>>(I.D);
+  k_scale_kinetic<<<I.ntiles, TILE, 0, I.stream>>>(I.D, sys, mode);
+  k_scale_velocities<<<nblocks(I.N, 256), 256, 0, I.stream>>>(I.D, sys, mode, target, dt_over_tau);
+  I.launched(3);
+  I.check_launch("scale_velocities");
+  // the drift already queued for the next step used the old velocities: redo it
+  I.pend = false;
+  CK(cudaStreamSynchronize(I.stream));
+}
+
 void Engine::set_active(int sys, bool on) {
   Impl& I = *d_;
   if (sys < 0 || sys >= I.nsys) throw Error(1, "system index out of range");

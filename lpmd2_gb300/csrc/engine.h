@@ -90,6 +90,8 @@ class Engine {
   void get_atoms(int sys, double* pos, double* vel, double* acc);
   // Inactive systems are skipped by every kernel; their state is left as it was.
   void set_active(int sys, bool on);
+  // Velocity rescaling between steps (mode 0: set temperature, 1: Berendsen); sys < 0: all.
+  void scale_velocities(int sys, int mode, double target, double dt_over_tau);
   // Lossless snapshot of the whole engine state; load needs an identically configured engine.
   size_t checkpoint_size();
   void checkpoint_save(void* buf, size_t bytes);

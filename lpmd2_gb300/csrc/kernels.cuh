@@ -416,6 +416,63 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
 // Integration: drift half of velocity Verlet
 // ---------------------------------------------------------------------------------------------
 
+// Velocity rescaling between steps.  The temperature is measured afresh, as the modifiers do:
+// k_kinetic_clear + k_scale_kinetic sum the kinetic energy of the current velocities into the
+// system's int64 kinetic slot (2^-44 units; each warp's FP64 sum rounded once, so the total is
+// order-independent), then k_scale_velocities scales.
+//   mode 0, SimulationBuilder::SetTemperature (liblpmd/simulation/simulationbuilder.cc:53-72,
+//     called by plugins/tempscaling.cc:66-71 and plugins/temperature.cc:58-62 with tag = "any
+//     atom has fixedvel/fixedpos"): T over the untagged atoms, tagged atoms keep their velocity,
+//     v *= sqrt(target / T);
+//   mode 1, BerendsenModifier::Apply (plugins/berendsen.cc:72-99): T over all atoms
+//     (lpmd::Temperature with tag false, liblpmd/lpmd/properties.h:40-53), every atom scaled by
+//     sqrt(1 + dt/tau * (target / T - 1)).
+// The kinetic slot is free between steps: the next force evaluation's decision clears it.
+// A system at T = 0 is left as it is (the reference would divide by zero).
+__global__ void k_kinetic_clear(Dev D) {
+  for (int s = threadIdx.x; s < D.nsys; s += blockDim.x) D.sys_acc[(long long)s * SA_LEN + SA_KE] = 0ull;
+}
+
+__global__ void __launch_bounds__(TILE) k_scale_kinetic(Dev D, int sys, int mode) {
+  const int tile = blockIdx.x;
+  const int s = D.tile_sys[tile];
+  if ((sys >= 0 && s != sys) || !D.sysd[s].active) return;  // whole block: one tile, one system
+  const long long i = D.tile_first[tile] + threadIdx.x;
+  double ke = 0.0;
+  if ((int)threadIdx.x < D.tile_count[tile] &&
+      !(mode == 0 && D.has_flags && (D.flags[i] & (FLAG_FIXEDVEL | FLAG_FIXEDPOS)))) {
+    const double vx = D.vx[i], vy = D.vy[i], vz = D.vz[i];
+    ke = dmul(dmul(0.5, D.mass[i]), ref_sq(vx, vy, vz));
+  }
+  const double kw = warp_sum(ke);
+  __shared__ long long part[TILE / 32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = __double2ll_rn(kw * FIX_KE);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    for (int w = 0; w < TILE / 32; ++w) t += part[w];
+    atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_KE, (unsigned long long)t);
+  }
+}
+
+__global__ void k_scale_velocities(Dev D, int sys, int mode, double target, double dt_over_tau) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.N) return;
+  const int s = D.sysid[i];
+  const SysDev& S = D.sysd[s];
+  if ((sys >= 0 && s != sys) || !S.active) return;
+  const double KIN2EV = 103.64269, KBOLTZMANN = 8.6173422E-05;  // liblpmd/lpmd/properties.h:10-11
+  const double ke = (double)(long long)__ldcg(D.sys_acc + (long long)s * SA_LEN + SA_KE) * (1.0 / FIX_KE);
+  const double kbn = mode == 0 ? S.kbn : dmul(KBOLTZMANN, (double)S.natoms);
+  const double T = ddiv(dmul(2.0 / 3.0, dmul(ke, KIN2EV)), kbn);
+  if (!(T > 0.0)) return;
+  if (mode == 0 && D.has_flags && (D.flags[i] & (FLAG_FIXEDVEL | FLAG_FIXEDPOS))) return;
+  const double f = mode == 0 ? sqrt(ddiv(target, T)) : sqrt(dadd(1.0, dmul(dt_over_tau, dsub(ddiv(target, T), 1.0))));
+  D.vx[i] = dmul(D.vx[i], f);
+  D.vy[i] = dmul(D.vy[i], f);
+  D.vz[i] = dmul(D.vz[i], f);
+}
+
 // Centre of every Verlet-list cell: ((c + 1/2) * d) per axis, FP64.
 __global__ void k_cell_centres(Dev D) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;

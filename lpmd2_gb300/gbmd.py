@@ -116,6 +116,9 @@ _SIGS = {
     "gbmd_batch_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "gbmd_batch_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "gbmd_batch_set_active": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int]),
+    "gbmd_sim_scale_velocities": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+    "gbmd_batch_scale_velocities": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                    ctypes.c_double]),
     "gbmd_sim_checkpoint_size": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     "gbmd_sim_checkpoint_save": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
     "gbmd_sim_checkpoint_load": (ctypes.c_int, [_VP, ctypes.c_void_p, ctypes.c_size_t]),
@@ -332,6 +335,14 @@ class Simulation:
         mc = None if mass is None else np.ascontiguousarray(np.broadcast_to(mass, (self.n,)), dtype=np.float64)
         _check(self.lib.gbmd_sim_set_atoms(self.h, _p(pos), _p(vel), _p(acc), _p(Zc, _I32), _p(mc)))
 
+    def set_temperature(self, target: float):
+        """SetTemperature (tempscaling, temperature): v *= sqrt(target / T) for untagged atoms."""
+        _check(self.lib.gbmd_sim_scale_velocities(self.h, 0, float(target), 0.0))
+
+    def berendsen(self, target: float, dt_over_tau: float):
+        """One Berendsen rescaling: v *= sqrt(1 + dt/tau (target / T - 1))."""
+        _check(self.lib.gbmd_sim_scale_velocities(self.h, 1, float(target), float(dt_over_tau)))
+
     def checkpoint(self) -> bytes:
         """Lossless snapshot of the whole state (gbmd_sim_checkpoint_save)."""
         return _checkpoint(self.lib, "sim", self.h)
@@ -458,6 +469,14 @@ class Batch:
 
     def set_active(self, sys: int, active: bool):
         _check(self.lib.gbmd_batch_set_active(self.h, sys, 1 if active else 0))
+
+    def set_temperature(self, target: float, sys: int = -1):
+        """Simulation.set_temperature for one system (-1: every active system)."""
+        _check(self.lib.gbmd_batch_scale_velocities(self.h, sys, 0, float(target), 0.0))
+
+    def berendsen(self, target: float, dt_over_tau: float, sys: int = -1):
+        """Simulation.berendsen for one system (-1: every active system)."""
+        _check(self.lib.gbmd_batch_scale_velocities(self.h, sys, 1, float(target), float(dt_over_tau)))
 
     def atoms(self, sys: int):
         n = int(self.natoms[sys])

@@ -90,3 +90,56 @@ def test_missing_components_are_reported():
     ctl = C.parse("cell cubic 20\ninput crystal3d type=fcc symbol=Ar nx=2 ny=2 nz=2\nsteps 1\n")
     with pytest.raises(C.ControlError, match="MissingComponent: cellmanager"):
         C.run(ctl)
+
+
+MODS = """
+steps 60
+use velocityverlet
+    dt 2.0
+enduse
+integrator velocityverlet
+use tempscaling as ramp
+    from 100
+    to 200
+enduse
+use temperature as fix
+    t 77
+enduse
+use berendsen
+    from 300
+    to 300
+    tau 8
+    start 12
+enduse
+use gdr
+enduse
+apply ramp each=20
+apply fix start=5 end=5
+apply berendsen each=40
+apply gdr each=10
+"""
+
+
+def test_modifier_schedule_follows_the_steppers():
+    ctl = C.parse(MODS)
+    assert set(ctl.modifiers) == {"ramp", "fix", "berendsen"}
+    assert any(s.startswith("apply gdr") for s in ctl.skipped)
+    sched = C.modifier_schedule(ctl, 2.0)
+    # tempscaling: ValueAtStep with end -1 replaced by the step count (lpmd/application.cc:443-444)
+    ramp = [(k, t) for k, mode, t, _ in sched if mode == 0 and t != 77.0]
+    assert ramp == [(20, 100 + 20 / 60 * 100), (40, 100 + 40 / 60 * 100), (60, 200.0)]
+    assert [(k, t) for k, mode, t, _ in sched if t == 77.0] == [(5, 77.0)]
+    # berendsen: switched on at step 12 (no rescaling), every step until 12 + tau/dt = 16, off at
+    # 17 with its own period restored; next active step 52 -> on, 53..56 rescale, off at 57
+    ber = [(k, dtt) for k, mode, _, dtt in sched if mode == 1]
+    assert [k for k, _ in ber] == [13, 14, 15, 16, 53, 54, 55, 56]
+    assert all(d == 2.0 / 8.0 for _, d in ber)
+    # same-step modifiers run in the order of their apply statements
+    assert [k for k, *_ in sched] == sorted(k for k, *_ in sched)
+
+
+def test_apply_of_an_unused_module_is_skipped_and_strict_rejects_it():
+    with pytest.raises(C.ControlError):
+        C.parse("steps 1\napply nothing each=2\n", strict=True)
+    ctl = C.parse("steps 1\napply nothing each=2\n")
+    assert ctl.applies == [] and ctl.skipped

@@ -8,6 +8,7 @@ simulation it describes through libgbmd:
 
   cell cubic a [scale] | cell crystal a b c 90 90 90 [scale]    orthogonal periodic box
   input crystal3d type=fcc|bcc|sc|hcp symbol=X nx= ny= nz=     initial lattice (crystal3d)
+  input module=lpmd|xyz file=F                                 first configuration of a file
   prepare temperature t=T [seed=S]                             velocities (see below)
   use linkedcell|verletlist|minimumimage|lennardjones|suttonchen|finnissinclair|
       finnissinclair-ext|velocityverlet [as id] ... enduse     the timestep's plugins
@@ -15,7 +16,9 @@ simulation it describes through libgbmd:
   steps N                                                      velocity-Verlet steps
   monitor p1,p2,... [start= end= each= output=]                thermo columns (monitor.cc)
   use tempscaling|temperature|berendsen ... enduse; apply <id>  thermostats between steps
-  output xyz <file> [each= start= end= level=]                 XYZ frames (xyz.cc)
+  output xyz <file> [each= start= end= level= precout=]        XYZ frames (xyz.cc)
+  output module=lpmd file=F [level= type=lpmd|zlp blocksize= compression= extra=TYPE]
+                                                               lpmd / zlp frames (lpmd.cc)
   mass <symbol> <value>, set <option> <value>, periodic x y z
 
 Thermo comes from the device's per-step record, so monitored steps cost no extra
@@ -40,6 +43,7 @@ from typing import TextIO
 
 import numpy as np
 
+from . import formats as F
 from . import inputs as I
 
 TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "finnissinclair",
@@ -316,15 +320,37 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         raise ControlError("no cell statement")
     if not all(ctl.periodic):
         raise ControlError("the GPU path runs fully periodic cells only")
-    if ctl.input is None or ctl.input.get("module") != "crystal3d":
-        raise ControlError("input: only the crystal3d generator runs on the GPU path")
-    inp = ctl.input
-    Z, mass = _species(inp.get("symbol", "H"), ctl)
-    pos = crystal3d(inp.get("type", "fcc"), int(inp.get("nx", 1)), int(inp.get("ny", 1)), int(inp.get("nz", 1)),
-                    ctl.cell)
-    n = len(pos)
-    masses = np.full(n, mass)
-    vel = np.zeros((n, 3))
+    inp = ctl.input or {}
+    cell = np.asarray(ctl.cell, dtype=np.float64)
+    if inp.get("module") == "crystal3d":
+        symbols = inp.get("symbol", "H")
+        Z, mass = _species(symbols, ctl)
+        pos = crystal3d(inp.get("type", "fcc"), int(inp.get("nx", 1)), int(inp.get("ny", 1)), int(inp.get("nz", 1)),
+                        cell)
+        n = len(pos)
+        masses = np.full(n, mass)
+        vel = np.zeros((n, 3))
+    elif inp.get("module") in ("lpmd", "xyz"):
+        # CellReader::ReadCell of the first configuration (Application::FillAtomsFromCellReader,
+        # lpmd/application.cc:207-237); accelerations are recomputed before the first step
+        path = Path(inp.get("file", ""))
+        path = path if path.is_absolute() else workdir / path
+        try:
+            fr = (F.read_lpmd(path) if inp["module"] == "lpmd" else F.read_xyz(path))[0]
+        except (OSError, ValueError, IndexError, KeyError) as e:
+            raise ControlError(f"input {inp['module']}: {e}") from None
+        if inp["module"] == "lpmd" and _true(ctl.options.get("replacecell", "false")):
+            cell = np.asarray(fr["L"], dtype=np.float64)
+        pos, vel = fr["pos"], fr["vel"]
+        if inp["module"] == "xyz" and not ((pos >= 0.0) & (pos < cell)).all():
+            raise ControlError("input xyz: an atom was found outside the cell")  # external=consider
+        n = len(pos)
+        table = {s: _species(s, ctl) for s in set(fr["symbols"])}
+        Z = np.array([table[s][0] for s in fr["symbols"]], dtype=np.int32)
+        masses = np.array([table[s][1] for s in fr["symbols"]])
+        symbols = fr["symbols"][0] if len(table) == 1 else fr["symbols"]
+    else:
+        raise ControlError("input: the crystal3d generator and lpmd/zlp/xyz files run on the GPU path")
     for pr in ctl.prepares:
         if pr.get("module") != "temperature":
             raise ControlError(f"prepare {pr.get('module')}: not supported on the GPU path")
@@ -342,7 +368,7 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         raise ControlError("MissingComponent: potential")
     if ctl.integrator is None:
         raise ControlError("MissingComponent: integrator")
-    sim = gbmd.Simulation(n, ctl.cell, device=device)
+    sim = gbmd.Simulation(n, cell, device=device)
     sim.set_atoms(pos, vel, Z=Z, mass=masses)
     sim.set_cell_manager(plugin(ctl.cellmanager, "cellmanager"))
     for uid, a, b in ctl.potentials:
@@ -364,20 +390,18 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         monitors.append((props, int(m.get("start", 0)), int(m.get("end", -1)), max(1, int(m.get("each", 1))), stream))
     outputs = []
     for o in ctl.outputs:
-        if o.get("module") != "xyz":
-            raise ControlError(f"output {o.get('module')}: only xyz frames are written on the GPU path")
-        outputs.append((open(workdir / o["file"], "w"), int(o.get("start", 0)), int(o.get("end", -1)),
-                        max(1, int(o.get("each", 1))), int(o.get("level", 0))))
-    symbol = inp.get("symbol", "H")
+        kw = {k: v for k, v in o.items() if k not in ("module", "file", "start", "end", "each")}
+        try:
+            w = F.open_writer(o.get("module", ""), workdir / o.get("file", "noname"), **kw)
+        except (ValueError, TypeError) as e:
+            raise ControlError(f"output {o.get('module')}: {e}") from None
+        w.write_header()  # Application::OpenOutputStreams (lpmd/application.cc:537-556)
+        outputs.append((w, int(o.get("start", 0)), int(o.get("end", -1)), max(1, int(o.get("each", 1))), None))
     rows = []
 
-    def emit_frame(f, level):
+    def emit_frame(w, _):
         p, v, a = sim.atoms()
-        f.write(f"{n}\n\n")
-        cols = [p] + ([v] if level >= 1 else []) + ([a] if level >= 2 else [])
-        data = np.hstack(cols)
-        for r in data:
-            f.write(symbol + " " + " ".join(f"{x:.8f}" for x in r) + "\n")
+        w.write_frame(symbols, cell, p, v, a)
 
     dt = float(_kv(ctl.uses[ctl.integrator][1]).get("dt", "1.0"))
     schedule = modifier_schedule(ctl, dt)
@@ -411,7 +435,7 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
             tags = None
             for props, st, en, ev, stream in monitors:
                 if _active(step, st, en, ev):
-                    tags = tags or _tags(rec, n, ctl.cell, masses)
+                    tags = tags or _tags(rec, n, cell, masses)
                     vals = []
                     for p in props:
                         if p not in tags:
@@ -425,8 +449,8 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
     for *_, stream in monitors:
         if stream is not out:
             stream.close()
-    for f, *_ in outputs:
-        f.close()
+    for w, *_ in outputs:
+        w.close()
     p, v, a = sim.atoms()
     th = sim.thermo()
     sim.close()

@@ -269,6 +269,7 @@ def _ref():
         lib = ctypes.CDLL(str(REF_LIB))
         lib.ref_last_error.restype = ctypes.c_char_p
         lib.ref_run.restype = ctypes.c_int
+        lib.ref_write_frames.restype = ctypes.c_int
         _REF = lib
     return _REF
 
@@ -315,3 +316,19 @@ def run_reference(pos, L, symbol, vel, cm, cm_args, pots, dt, nsteps, neigh=None
         out["neigh_counts"] = counts
         out["neigh_idx"] = idx[: total.value]
     return out
+
+
+def write_reference_frames(path, module: str, args: str, L, Z, pos, vel=None, acc=None) -> None:
+    """Writes frames [nframes, n, 3] through the reference's own output plugin (lpmd / xyz,
+    see ref_driver.cpp); `args` must name `path` with its `file` keyword."""
+    lib = _ref()
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    nf, n = pos.shape[0], pos.shape[1]
+    vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
+    acc = None if acc is None else np.ascontiguousarray(acc, dtype=np.float64)
+    L = np.ascontiguousarray(L, dtype=np.float64)
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    rc = lib.ref_write_frames(ctypes.c_int64(n), _ptr(L), _ptr(Z, ctypes.POINTER(ctypes.c_int32)), ctypes.c_int64(nf),
+                              _ptr(pos), _ptr(vel), _ptr(acc), module.encode(), args.encode(), str(path).encode())
+    if rc:
+        raise OracleError("reference: " + lib.ref_last_error().decode())

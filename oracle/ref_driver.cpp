@@ -19,6 +19,8 @@
 #include <runtime/runtime_context.h>
 
 #include "finnissinclair-ext.h"
+#include "lpmd.h"
+#include "xyz.h"
 #include "finnissinclair.h"
 #include "lennardjones.h"
 #include "linkedcell.h"
@@ -31,6 +33,7 @@
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <fstream>
 #include <string>
 
 using namespace lpmd;
@@ -173,6 +176,59 @@ extern "C" int ref_run(int64_t n, const double* L, const char* symbol, const dou
         if (out_vel) out_vel[3 * i + q] = atoms[i].Velocity()[q];
         if (out_acc) out_acc[3 * i + q] = atoms[i].Acceleration()[q];
       }
+    return 0;
+  } catch (std::exception& e) {
+    std::snprintf(g_error, sizeof g_error, "%s", e.what());
+    return 1;
+  }
+}
+
+// Writes nframes configurations of n atoms through the reference's own output plugin (`module`
+// "lpmd" or "xyz", constructed with `args`, which name the file): CellWriter::WriteHeader once,
+// then WriteCell per frame (the calls Application::OpenOutputStreams and
+// SaveCurrentConfiguration make, lpmd/application.cc:537-578).  Frames are [nframes][n][3];
+// vel/acc may be NULL (zeros).  Returns 0, or 1 with the message in ref_last_error().
+extern "C" int ref_write_frames(int64_t n, const double* L, const int32_t* Z, int64_t nframes,
+                                const double* pos, const double* vel, const double* acc,
+                                const char* module, const char* args, const char* path) {
+  g_error[0] = 0;
+  try {
+    static RuntimeContext context;
+    Simulation& md = SimulationBuilder::CreateFixedOrthogonal(context, long(n), Atom("H"));
+    BasicCell& cell = md.Cell();
+    cell[0] = L[0] * e1;
+    cell[1] = L[1] * e2;
+    cell[2] = L[2] * e3;
+    BasicParticleSet& atoms = md.Atoms();
+    LPMDFormat* lp = nullptr;
+    XYZFormat* xy = nullptr;
+    CellWriter* w = nullptr;
+    if (std::string(module) == "lpmd")
+      w = lp = new LPMDFormat(args);
+    else if (std::string(module) == "xyz")
+      w = xy = new XYZFormat(args);
+    else {
+      std::snprintf(g_error, sizeof g_error, "unknown output module %s", module);
+      return 1;
+    }
+    {
+      std::ofstream os(path, std::ios::binary);
+      w->WriteHeader(os, nullptr);
+      for (int64_t f = 0; f < nframes; ++f) {
+        const int64_t b = f * n * 3;
+        for (long i = 0; i < atoms.Size(); ++i) {
+          atoms[i].Z() = Z[i];
+          atoms[i].Position() = Vector(pos[b + 3 * i], pos[b + 3 * i + 1], pos[b + 3 * i + 2]);
+          atoms[i].Velocity() =
+              vel ? Vector(vel[b + 3 * i], vel[b + 3 * i + 1], vel[b + 3 * i + 2]) : Vector(0.0, 0.0, 0.0);
+          atoms[i].Acceleration() =
+              acc ? Vector(acc[b + 3 * i], acc[b + 3 * i + 1], acc[b + 3 * i + 2]) : Vector(0.0, 0.0, 0.0);
+        }
+        w->WriteCell(os, md);
+      }
+    }
+    delete lp;
+    delete xy;
     return 0;
   } catch (std::exception& e) {
     std::snprintf(g_error, sizeof g_error, "%s", e.what());

@@ -68,3 +68,89 @@ def test_config1_control_file_matches_reference_run(tmp_path):
     assert len((tmp_path / "monitor.dat").read_text().splitlines()) == 100
     xyz = (tmp_path / "last.xyz").read_text().splitlines()
     assert int(xyz[0]) == 4000 and len(xyz) == 4002 and xyz[2].startswith("Ar ")
+
+
+CU_TEXT = """
+cell crystal 14.44
+input crystal3d type=fcc symbol=Cu nx=4 ny=4 nz=4
+output module=lpmd file=cu.zlp level=2 each=50
+output xyz cu.xyz level=1 each=100
+monitor step,temperature,total-energy start=0 each=10 end=-1 output=props.dat
+prepare temperature t=300
+steps 100
+use velocityverlet
+ dt 1.0
+enduse
+use suttonchen
+ e 0.015713
+ n 9.0
+ m 6.0
+ a 3.61
+ c 39.755
+ cutoff 6.0
+enduse
+use linkedcell
+ cutoff 7.0
+ mode auto
+enduse
+use tempscaling
+ from 300.0
+ to 300.0
+enduse
+potential suttonchen Cu Cu
+integrator velocityverlet
+cellmanager linkedcell
+apply tempscaling start=0 end=100 each=20
+"""
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sutton_chen_control_file_with_thermostat_and_frames(precision, tmp_path):
+    from lpmd2_gb300 import formats as F
+
+    ctl = C.parse(CU_TEXT, strict=True)
+    np.testing.assert_array_equal(ctl.cell, [14.44, 14.44, 14.44])  # `cell crystal a` is cubic
+    out = C.run(ctl, precision=precision, workdir=tmp_path)
+    n = out["natoms"]
+    m = np.full(n, C.STANDARD_MASS["Cu"])
+    ke = 0.5 * np.sum(m * np.sum(out["vel"] ** 2, axis=1)) * 103.64269
+    assert abs((2.0 / 3.0) * ke / (8.6173422e-05 * n) / 300.0 - 1.0) < 1e-11  # rescaled at step 100
+    frames = F.read_lpmd(tmp_path / "cu.zlp")
+    assert len(frames) == 2 and all(f["symbols"] == ["Cu"] * n for f in frames)
+    last = frames[-1]
+    assert np.abs(last["pos"] - out["pos"]).max() <= 0.5e-6 * 14.44 * (1 + 1e-9)
+    # the frame is written after the modifier (SaveCurrentConfiguration follows RunModifiers)
+    assert np.abs(last["vel"] - out["vel"]).max() <= 0.5e-6 * (1 + 1e-9)
+    assert np.abs(last["acc"] - out["acc"]).max() <= 0.5e-6 * (1 + 1e-9)
+    xyz = F.read_xyz(tmp_path / "cu.xyz")
+    assert len(xyz) == 1 and xyz[0]["level"] == 1
+    assert np.abs(xyz[0]["pos"] - out["pos"]).max() <= 0.5e-8 * 16
+    rows = np.loadtxt(tmp_path / "props.dat")
+    assert list(rows[:, 0]) == list(range(10, 101, 10))
+
+
+def test_input_from_an_lpmd_file(tmp_path):
+    from lpmd2_gb300 import formats as F
+
+    g = load_golden("lj_config1")
+    L = np.asarray(g["L"], float)
+    w = F.LPMDWriter(tmp_path / "start.lpmd", level=1)
+    w.write_header()
+    w.write_frame("Ar", L, g["pos_in"], g["vel_in"])
+    w.close()
+    text = control_text(float(L[0])).replace("input crystal3d type=fcc symbol=Ar nx=10 ny=10 nz=10",
+                                             "input module=lpmd file=start.lpmd")
+    text = text.replace("prepare temperature t=100.0 seed=1\n", "")
+    out = C.run(C.parse(text, strict=True), precision="fp64", workdir=tmp_path)
+    fr = F.read_lpmd(tmp_path / "start.lpmd")[0]
+    sim = gbmd.Simulation(len(fr["pos"]), L)
+    sim.set_atoms(fr["pos"], fr["vel"], Z=g["Z"], mass=g["mass"])
+    sim.set_cell_manager(gbmd.Plugin("linkedcell", "cutoff 8.5 nx 6 ny 6 nz 6"))
+    sim.add_potential(gbmd.Plugin("lennardjones", "sigma 3.405 epsilon 0.0103 cutoff 8.5"), 18, 18)
+    sim.set_integrator(gbmd.Plugin("velocityverlet", "dt 1.0"))
+    sim.set_precision("fp64")
+    sim.update_forces()
+    sim.do_steps(100)
+    p, v, _ = sim.atoms()
+    np.testing.assert_array_equal(out["pos"], p)
+    np.testing.assert_array_equal(out["vel"], v)

@@ -10,7 +10,7 @@ simulation it describes through libgbmd:
   input crystal3d type=fcc|bcc|sc|hcp symbol=X nx= ny= nz=     initial lattice (crystal3d)
   input module=lpmd|xyz file=F                                 first configuration of a file
   prepare temperature t=T [seed=S]                             velocities (see below)
-  use linkedcell|verletlist|minimumimage|lennardjones|suttonchen|finnissinclair|
+  use linkedcell|verletlist|minimumimage|lennardjones|suttonchen|gupta|finnissinclair|
       finnissinclair-ext|velocityverlet [as id] ... enduse     the timestep's plugins
   cellmanager <id> / potential <id> A B / integrator <id>      wiring (ids of use blocks)
   steps N                                                      velocity-Verlet steps
@@ -46,7 +46,7 @@ import numpy as np
 from . import formats as F
 from . import inputs as I
 
-TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "finnissinclair",
+TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "gupta", "finnissinclair",
                     "finnissinclair-ext", "velocityverlet"}
 MODIFIER_PLUGINS = {"tempscaling", "temperature", "berendsen"}
 SKIPPED_STATEMENTS = {"property", "visualize", "filter", "average", "bond", "charge", "plugindir"}

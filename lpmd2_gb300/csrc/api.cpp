@@ -73,7 +73,7 @@ PotParams finalize_potential(int kind, const double* v, int s1, int s2) {
   P.kind = kind;
   P.spc_sum = s1 + s2;
   P.int_n = P.int_m = -1;
-  int np = (kind == POT_LJ) ? 3 : (kind == POT_SC) ? 6 : (kind == POT_FS) ? 7 : 9;
+  int np = (kind == POT_LJ) ? 3 : (kind == POT_SC || kind == POT_GUPTA) ? 6 : (kind == POT_FS) ? 7 : 9;
   for (int k = 0; k < np; ++k) P.p[k] = v[k];
   if (kind == POT_LJ) {
     P.cutoff = v[2];
@@ -93,6 +93,15 @@ PotParams finalize_potential(int kind, const double* v, int s1, int s2) {
     P.f[1] = (float)(-n * e * P.an);
     P.f[2] = (float)(0.5 * m * c * e * P.am);
     P.f[3] = (float)P.am;
+  } else if (kind == POT_GUPTA) {
+    const double A = v[0], r0 = v[1], p = v[2], B = v[3], q = v[4];
+    P.cutoff = v[5];  // plugins/gupta.cc:26
+    P.f[0] = (float)A;
+    P.f[1] = (float)(-p / r0);
+    P.f[2] = (float)(-(A * p / r0));
+    P.f[3] = (float)(B * q / r0);
+    P.f[4] = (float)(-2.0 * q / r0);
+    P.f[5] = (float)r0;
   } else {
     double c = (kind == POT_FS) ? v[5] : v[7];
     double d = (kind == POT_FS) ? v[6] : v[8];
@@ -173,15 +182,17 @@ PluginSpec make_plugin(const std::string& name, const std::string& args) {
     p.cm.kind = CM_MINIMUMIMAGE;
     p.cm.cutoff = num(p, "cutoff");
   } else if (name == "lennardjones" || name == "suttonchen" || name == "finnissinclair" ||
-             name == "finnissinclair-ext") {
+             name == "finnissinclair-ext" || name == "gupta") {
     p.kind = GBMD_KIND_POTENTIAL;
     static const char* lj[] = {"sigma", "epsilon", "cutoff"};
     static const char* sc[] = {"e", "a", "n", "m", "c", "cutoff"};
     static const char* fs[] = {"c0", "c1", "c2", "A", "B", "c", "d"};
     static const char* fx[] = {"c0", "c1", "c2", "c3", "c4", "A", "B", "c", "d"};
-    int kind = name == "lennardjones" ? POT_LJ : name == "suttonchen" ? POT_SC : name == "finnissinclair" ? POT_FS : POT_FSEXT;
-    const char** keys = kind == POT_LJ ? lj : kind == POT_SC ? sc : kind == POT_FS ? fs : fx;
-    int nk = kind == POT_LJ ? 3 : kind == POT_SC ? 6 : kind == POT_FS ? 7 : 9;
+    static const char* gu[] = {"A", "r0", "p", "B", "q", "cutoff"};  // plugins/gupta.cc:14-19
+    int kind = name == "lennardjones" ? POT_LJ : name == "suttonchen" ? POT_SC : name == "finnissinclair" ? POT_FS
+             : name == "gupta" ? POT_GUPTA : POT_FSEXT;
+    const char** keys = kind == POT_LJ ? lj : kind == POT_SC ? sc : kind == POT_FS ? fs : kind == POT_GUPTA ? gu : fx;
+    int nk = kind == POT_LJ ? 3 : (kind == POT_SC || kind == POT_GUPTA) ? 6 : kind == POT_FS ? 7 : 9;
     if (kind == POT_SC) defaulted("corrections", "false");
     double v[10] = {0};
     for (int k = 0; k < nk; ++k) v[k] = num(p, keys[k]);
@@ -227,6 +238,7 @@ void potential_eval(const PotParams& P, int what, const double* a, double* out) 
     return;
   }
   auto rho_of = [&](double r) {
+    if (P.kind == POT_GUPTA) return std::exp(-2.0e0 * v[4] * (r - v[1]) / v[1]);  // gupta.cc:56
     if (P.kind == POT_SC) return P.am * std::pow(1 / r, v[3]);
     if (P.kind == POT_FS) {
       const double B = v[4], d = v[6];
@@ -238,7 +250,9 @@ void potential_eval(const PotParams& P, int what, const double* a, double* out) 
   };
   if (what == 0) {
     double r = a[0];
-    if (P.kind == POT_SC) {
+    if (P.kind == POT_GUPTA) {
+      out[0] = v[0] * std::exp(-v[2] * (r - v[1]) / v[1]);  // gupta.cc:54
+    } else if (P.kind == POT_SC) {
       out[0] = v[0] * P.an * std::pow(1 / r, v[2]);
     } else if (P.kind == POT_FS) {
       const double c0 = v[0], c1 = v[1], c2 = v[2], c = v[5];
@@ -251,14 +265,16 @@ void potential_eval(const PotParams& P, int what, const double* a, double* out) 
   } else if (what == 2) {
     out[0] = rho_of(a[0]);
   } else if (what == 3) {
-    double A = P.kind == POT_SC ? v[4] * v[0] : P.kind == POT_FS ? v[3] : v[5];
+    double A = P.kind == POT_SC ? v[4] * v[0] : (P.kind == POT_FS || P.kind == POT_GUPTA) ? v[3] : v[5];
     out[0] = P.kind == POT_SC ? -v[4] * v[0] * std::sqrt(a[0]) : -A * std::sqrt(a[0]);
   } else if (what == 1 || what == 4) {
     double r = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
     double nrm[3] = {a[0] / r, a[1] / r, a[2] / r};
     double s = 0.0;
     if (what == 1) {
-      if (P.kind == POT_SC) {
+      if (P.kind == POT_GUPTA) {  // gupta.cc:60-62
+        s = -(v[0] * v[2] / v[1]) * std::exp(-v[2] * (r - v[1]) / v[1]);
+      } else if (P.kind == POT_SC) {
         double ir = 1.0e0 / r;
         s = -v[2] * v[0] * P.an * std::pow(ir, v[2] + 1);
       } else if (P.kind == POT_FS) {
@@ -274,7 +290,10 @@ void potential_eval(const PotParams& P, int what, const double* a, double* out) 
       }
     } else {
       const double rhoi = a[3], rhoj = a[4];
-      if (P.kind == POT_SC) {
+      if (P.kind == POT_GUPTA) {  // gupta.cc:64-70
+        s = (v[3] * v[4] / v[1]) * ((1.0e0 / std::sqrt(rhoi)) + (1.0e0 / std::sqrt(rhoj))) *
+            std::exp(-2.0e0 * v[4] * (r - v[1]) / v[1]);
+      } else if (P.kind == POT_SC) {
         double ir = 1.0e0 / r;
         s = 0.5 * v[3] * v[4] * v[0] * ((1 / std::sqrt(rhoi)) + 1 / (std::sqrt(rhoj))) * P.am * std::pow(ir, v[3] + 1);
       } else if (P.kind == POT_FS) {

@@ -55,6 +55,10 @@ __device__ __forceinline__ void lj_pair64(const PotParams& P, double r2, double&
 
 // rhoij(r) for the EAM density pass.
 __device__ __forceinline__ double eam_rho64(const PotParams& P, double r) {
+  if (P.kind == POT_GUPTA) {  // plugins/gupta.cc:56: exp(-2 q (r - r0) / r0)
+    const double r0 = P.p[1], q = P.p[4];
+    return exp(ddiv(dmul(dmul(-2.0, q), dsub(r, r0)), r0));
+  }
   if (P.kind == POT_SC) {
     double ir = ddiv(1.0, r);
     double pw = (P.int_m >= 0) ? ipow_d(ir, P.int_m) : pow(ir, P.p[3]);
@@ -81,7 +85,7 @@ __device__ __forceinline__ void eam_embed64(const PotParams& P, double rho, doub
   double sq = sqrt(rho);
   if (P.kind == POT_SC)
     F = dmul(dmul(-P.p[4], P.p[0]), sq);
-  else if (P.kind == POT_FS)
+  else if (P.kind == POT_FS || P.kind == POT_GUPTA)  // FS: -A sqrt(rho); Gupta: -B sqrt(rho)
     F = dmul(-P.p[3], sq);
   else
     F = dmul(-P.p[5], sq);
@@ -91,7 +95,17 @@ __device__ __forceinline__ void eam_embed64(const PotParams& P, double rho, doub
 // Pair energy V(r) and the scalar s with PairForce + ManyBodies = s * r^ (r^ = r_ij / r).
 __device__ __forceinline__ void eam_pair64(const PotParams& P, double r, double phi_i, double phi_j,
                                            double& s, double& e) {
-  if (P.kind == POT_SC) {
+  if (P.kind == POT_GUPTA) {
+    // plugins/gupta.cc:54,60-70: V = A exp(-p (r - r0) / r0), PairForce = -(A p / r0) exp(..),
+    // ManyBodies = (B q / r0) (1/sqrt(rho_i) + 1/sqrt(rho_j)) exp(-2 q (r - r0) / r0)
+    const double A = P.p[0], r0 = P.p[1], pp = P.p[2], B = P.p[3], q = P.p[4];
+    const double dr = dsub(r, r0);
+    const double ex = exp(ddiv(dmul(-pp, dr), r0));
+    e = dmul(A, ex);
+    const double pf = dmul(-ddiv(dmul(A, pp), r0), ex);
+    const double mb = dmul(dmul(ddiv(dmul(B, q), r0), dadd(phi_i, phi_j)), exp(ddiv(dmul(dmul(-2.0, q), dr), r0)));
+    s = dadd(pf, mb);
+  } else if (P.kind == POT_SC) {
     const double eps = P.p[0], n = P.p[2], m = P.p[3], c = P.p[4];
     double ir = ddiv(1.0, r);
     double irn = (P.int_n >= 0) ? ipow_d(ir, P.int_n) : pow(ir, n);
@@ -151,6 +165,7 @@ __device__ __forceinline__ void eam_pair64(const PotParams& P, double r, double 
 //   LJ: f[0]=sigma^2, f[1]=48 eps, f[2]=24 eps, f[3]=4 eps
 //   SC: f[0]=e*an, f[1]=-n*e*an, f[2]=0.5*m*c*e*am, f[3]=am
 //   FS/FSX: f[0..4]=c0..c4, f[5]=A, f[6]=B, f[7]=c, f[8]=d
+//   Gupta: f[0]=A, f[1]=-p/r0, f[2]=-A p/r0, f[3]=B q/r0, f[4]=-2q/r0, f[5]=r0
 // ------------------------------------------------------------------------------------------
 
 // g with F_i = g * r_ij, and the pair energy e; inv = 1/r^2.
@@ -162,6 +177,7 @@ __device__ __forceinline__ void lj_pair32(const PotParams& P, float inv, float& 
 }
 
 __device__ __forceinline__ float eam_rho32(const PotParams& P, float r2) {
+  if (P.kind == POT_GUPTA) return expf(P.f[4] * (r2 * rsqrtf(r2) - P.f[5]));
   if (P.kind == POT_SC) {
     if (P.int_m >= 0 && (P.int_m & 1) == 0) return P.f[3] * ipow_f(__frcp_rn(r2), P.int_m >> 1);
     float ir = rsqrtf(r2);
@@ -195,7 +211,12 @@ __device__ __forceinline__ float ipow_c(float x) {
 // s with F_i = s * r_ij (note: r_ij, not r^) and pair energy e.
 __device__ __forceinline__ void eam_pair32(const PotParams& P, float r2, float phi_i, float phi_j, float& s,
                                            float& e) {
-  if (P.kind == POT_SC) {
+  if (P.kind == POT_GUPTA) {
+    const float ir = rsqrtf(r2), dr = r2 * ir - P.f[5];
+    const float ex = expf(P.f[1] * dr);
+    e = P.f[0] * ex;
+    s = (P.f[2] * ex + P.f[3] * (phi_i + phi_j) * expf(P.f[4] * dr)) * ir;
+  } else if (P.kind == POT_SC) {
     float ir = rsqrtf(r2);
     float irn = (P.int_n >= 0) ? ipow_f(ir, P.int_n) : __powf(ir, (float)P.p[2]);
     float irm1 = (P.int_m >= 0) ? ipow_f(ir, P.int_m + 1) : __powf(ir, (float)P.p[3] + 1.0f);

@@ -17,8 +17,8 @@ KBOLTZMANN = 8.6173422e-05  # liblpmd/lpmd/properties.h:11
 FORCEFACTOR = 0.00964853  # session string "0.00964853", liblpmd/runtime/session.cc:17-31
 
 # Masses of the species used by the standard workloads (liblpmd/support/elements.cc:20-24).
-MASSES = {"Ar": 39.948, "Cu": 63.546, "Fe": 55.847, "Mo": 95.94}
-ATOMIC_NUMBERS = {"Ar": 18, "Cu": 29, "Fe": 26, "Mo": 42}
+MASSES = {"Ar": 39.948, "Cu": 63.546, "Fe": 55.847, "Mo": 95.94, "Au": 196.967}
+ATOMIC_NUMBERS = {"Ar": 18, "Cu": 29, "Fe": 26, "Mo": 42, "Au": 79}
 
 _M64 = (1 << 64) - 1
 

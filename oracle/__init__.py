@@ -20,12 +20,13 @@ THERMO_FIELDS = ["step", "epot", "ekin", "etot", "temperature", "virial", "px", 
                  "volume", "virial_pressure", "kinetic_pressure", "pressure"]
 
 CM_KIND = {"linkedcell": 1, "verletlist": 2, "minimumimage": 3}
-POT_KIND = {"lennardjones": 1, "suttonchen": 2, "finnissinclair": 3, "finnissinclair-ext": 4}
+POT_KIND = {"lennardjones": 1, "suttonchen": 2, "finnissinclair": 3, "finnissinclair-ext": 4, "gupta": 5}
 POT_KEYS = {
     "lennardjones": ["sigma", "epsilon", "cutoff"],
     "suttonchen": ["e", "a", "n", "m", "c", "cutoff"],
     "finnissinclair": ["c0", "c1", "c2", "A", "B", "c", "d"],
     "finnissinclair-ext": ["c0", "c1", "c2", "c3", "c4", "A", "B", "c", "d"],
+    "gupta": ["A", "r0", "p", "B", "q", "cutoff"],
 }
 ERRORS = {1: "invalid argument", 2: "maxneighbors is too small!", 3: "out of memory",
           4: "missing component", 5: "capacity"}

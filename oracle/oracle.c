@@ -501,8 +501,13 @@ static void lj_force(const orc_pot* p, const double r[3], double out[3]) {
 
 /* Metal functionals.  Sutton-Chen: plugins/suttonchen.cc:73-95; params {e,a,n,m,c,cutoff}.
  * Finnis-Sinclair: plugins/finnissinclair.cc:75-113; params {c0,c1,c2,A,B,c,d}.
- * Finnis-Sinclair-ext: plugins/finnissinclair-ext.cc:85-128; {c0,c1,c2,c3,c4,A,B,c,d}. */
+ * Finnis-Sinclair-ext: plugins/finnissinclair-ext.cc:85-128; {c0,c1,c2,c3,c4,A,B,c,d}.
+ * Gupta: plugins/gupta.cc:52-75; params {A,r0,p,B,q,cutoff}. */
 static double metal_pair_energy(const orc_pot* p, double r) {
+  if (p->kind == ORC_POT_GUPTA) {
+    const double A = p->p[0], r0 = p->p[1], pp = p->p[2];
+    return A * exp(-pp * (r - r0) / r0);
+  }
   if (p->kind == ORC_POT_SC) {
     const double e = p->p[0], n = p->p[2];
     double ir = 1 / r;
@@ -524,6 +529,10 @@ static double metal_pair_energy(const orc_pot* p, double r) {
 }
 
 static double metal_rhoij(const orc_pot* p, double r) {
+  if (p->kind == ORC_POT_GUPTA) {
+    const double r0 = p->p[1], q = p->p[4];
+    return exp(-2.0e0 * q * (r - r0) / r0);
+  }
   if (p->kind == ORC_POT_SC) {
     const double m = p->p[3];
     double ir = 1 / r;
@@ -544,6 +553,8 @@ static double metal_rhoij(const orc_pot* p, double r) {
 }
 
 static double metal_F(const orc_pot* p, double rhoi) {
+  if (p->kind == ORC_POT_GUPTA)
+    return -p->p[3] * sqrt(rhoi);
   if (p->kind == ORC_POT_SC) {
     const double e = p->p[0], c = p->p[4];
     return -c * e * sqrt(rhoi);
@@ -556,6 +567,10 @@ static double metal_F(const orc_pot* p, double rhoi) {
 
 /* PairForce(normrij, r): a scalar times normrij; the scalar is returned. */
 static double metal_pair_force(const orc_pot* p, double rmod) {
+  if (p->kind == ORC_POT_GUPTA) {
+    const double A = p->p[0], r0 = p->p[1], pp = p->p[2];
+    return -(A * pp / r0) * exp(-pp * (rmod - r0) / r0);
+  }
   if (p->kind == ORC_POT_SC) {
     const double e = p->p[0], n = p->p[2];
     double ir = 1.0e0 / rmod;
@@ -588,6 +603,10 @@ static double metal_pair_force(const orc_pot* p, double rmod) {
  * has_value tells whether the reference returns tmp*normrij (1) or Vector(0,0,0) (0); the
  * two differ only for -0.0 components, which do not change any sum. */
 static double metal_many_bodies(const orc_pot* p, double rhoi, double rhoj, double rmod) {
+  if (p->kind == ORC_POT_GUPTA) {
+    const double r0 = p->p[1], B = p->p[3], q = p->p[4];
+    return (B * q / r0) * ((1.0e0 / sqrt(rhoi)) + (1.0e0 / sqrt(rhoj))) * exp(-2.0e0 * q * (rmod - r0) / r0);
+  }
   if (p->kind == ORC_POT_SC) {
     const double e = p->p[0], m = p->p[3], c = p->p[4];
     double ir = 1.0e0 / rmod;
@@ -881,8 +900,8 @@ int orc_sim_set_minimumimage(orc_sim* s, double cutoff) {
 int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparams, int s1, int s2) {
   if (s->npots >= ORC_MAXPOT)
     return ORC_ERR_INVALID;
-  int need = (kind == ORC_POT_LJ) ? 3 : (kind == ORC_POT_SC) ? 6 : (kind == ORC_POT_FS) ? 7 : 9;
-  if (kind < ORC_POT_LJ || kind > ORC_POT_FSEXT || nparams < need)
+  int need = (kind == ORC_POT_LJ) ? 3 : (kind == ORC_POT_SC || kind == ORC_POT_GUPTA) ? 6 : (kind == ORC_POT_FS) ? 7 : 9;
+  if (kind < ORC_POT_LJ || kind > ORC_POT_GUPTA || nparams < need)
     return ORC_ERR_INVALID;
   orc_pot* p = &s->pots[s->npots];
   memset(p, 0, sizeof(*p));
@@ -896,6 +915,8 @@ int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparam
     p->cutoff = params[5];
     p->an = pow(params[1], params[2]); /* suttonchen.cc:29-30 */
     p->am = pow(params[1], params[3]);
+  } else if (kind == ORC_POT_GUPTA) {
+    p->cutoff = params[5]; /* gupta.cc:26 */
   } else if (kind == ORC_POT_FS) {
     double c = params[5], d = params[6];
     p->cutoff = (d >= c) ? d : c; /* finnissinclair.cc:27-30 */

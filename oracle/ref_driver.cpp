@@ -22,6 +22,7 @@
 #include "lpmd.h"
 #include "xyz.h"
 #include "finnissinclair.h"
+#include "gupta.h"
 #include "lennardjones.h"
 #include "linkedcell.h"
 #include "minimumimage.h"
@@ -57,6 +58,7 @@ Potential* make_pot(const std::string& name, const std::string& args) {
   if (name == "suttonchen") return new SuttonChen(args);
   if (name == "finnissinclair") return new FinnisSinclair(args);
   if (name == "finnissinclair-ext") return new FinnisSinclairExt(args);
+  if (name == "gupta") return new Gupta(args);
   return nullptr;
 }
 

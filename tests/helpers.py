@@ -14,6 +14,8 @@ LJ_AR = "sigma 3.405 epsilon 0.0103 cutoff 8.5"
 SC_CU = "e 0.012382 a 3.61 n 9 m 6 c 39.432 cutoff 7.22"
 # Finnis-Sinclair alpha-Fe (Finnis & Sinclair 1984) and an extended (quartic) variant.
 FS_FE = "c0 1.2371147 c1 -0.3592185 c2 -0.0385607 A 1.828905 B 1.8 c 3.40 d 3.569745"
+# Gupta / tight-binding second-moment gold (Cleri and Rosato, Phys. Rev. B 48, 22 (1993))
+GUPTA_AU = "A 0.2061 r0 2.884 p 10.229 B 1.790 q 4.036 cutoff 6.0"
 FSX_MO = "c0 47.1346499 c1 -33.7665655 c2 6.2541999 c3 -0.0122 c4 0.0001 A 1.848 B 0.5 c 3.25 d 4.1"
 
 
@@ -87,6 +89,13 @@ def workload(name: str) -> dict:
         return dict(pos=pos, L=L, symbol="Mo", Z=42, vel=I.maxwell_boltzmann(m, 300.0, seed=6),
                     cm="linkedcell", cm_args="cutoff 4.1 nx 4 ny 4 nz 4",
                     pots=[("finnissinclair-ext", FSX_MO, -1, -1)], dt=1.0, nsteps=10, neigh=(1, 4.1))
+    if name == "gupta_au":
+        pos, L = I.fcc_fast(6, 6, 6, 4.08)
+        pos = I.remove_sites(pos, 0.01, seed=8)
+        m = np.full(len(pos), I.MASSES["Au"])
+        return dict(pos=pos, L=L, symbol="Au", Z=79, vel=I.maxwell_boltzmann(m, 400.0, seed=8),
+                    cm="linkedcell", cm_args="cutoff 6.0 nx 4 ny 4 nz 4",
+                    pots=[("gupta", GUPTA_AU, -1, -1)], dt=2.0, nsteps=20, neigh=(1, 6.0))
     if name == "lj_auto":
         pos, L = I.fcc_crystal3d(10, 10, 10, 5.26)
         m = np.full(len(pos), I.MASSES["Ar"])
@@ -102,7 +111,7 @@ def workload(name: str) -> dict:
     raise KeyError(name)
 
 
-GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "lj_auto", "lj_nx2"]
+GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_auto", "lj_nx2"]
 
 
 def load_golden(name: str) -> dict:

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import FS_FE, FSX_MO, LJ_AR, SC_CU
+from helpers import FS_FE, FSX_MO, GUPTA_AU, LJ_AR, SC_CU
 from lpmd2_gb300 import gbmd
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -100,7 +100,8 @@ def test_lj_functionals_match_checker(r):
 
 
 @pytest.mark.parametrize("spec", [("suttonchen", SC_CU, 2.6), ("suttonchen", SC_CU, 5.1),
-                                  ("finnissinclair", FS_FE, 2.5), ("finnissinclair-ext", FSX_MO, 2.9)])
+                                  ("finnissinclair", FS_FE, 2.5), ("finnissinclair-ext", FSX_MO, 2.9),
+                                  ("gupta", GUPTA_AU, 2.7), ("gupta", GUPTA_AU, 4.9)])
 def test_metal_functionals_match_checker(spec):
     name, args, r = spec
     p = gbmd.Plugin(name, args)
@@ -119,3 +120,21 @@ def test_sutton_chen_closed_form():
     assert p.pair_energy(r) == pytest.approx(e * (a / r) ** n, rel=1e-14)
     assert p.rhoij(r) == pytest.approx((a / r) ** m, rel=1e-14)
     assert p.F(2.0) == pytest.approx(-c * e * math.sqrt(2.0), rel=1e-15)
+
+
+def test_gupta_closed_form():
+    # plugins/gupta.cc:52-70 (Cleri-Rosato second-moment form)
+    A, r0, pp, B, q = 0.2061, 2.884, 10.229, 1.790, 4.036
+    p = gbmd.Plugin("gupta", GUPTA_AU)
+    assert p.cutoff() == 6.0
+    r = 3.1
+    assert p.pair_energy(r) == pytest.approx(A * math.exp(-pp * (r / r0 - 1)), rel=1e-14)
+    assert p.rhoij(r) == pytest.approx(math.exp(-2 * q * (r / r0 - 1)), rel=1e-14)
+    assert p.F(2.0) == pytest.approx(-B * math.sqrt(2.0), rel=1e-15)
+    f = p.pair_force([r, 0.0, 0.0])
+    assert f[0] == pytest.approx(-(A * pp / r0) * math.exp(-pp * (r / r0 - 1)), rel=1e-14)
+    mb = p.many_bodies([0.0, r, 0.0], 2.0, 3.0)
+    want = (B * q / r0) * (1 / math.sqrt(2.0) + 1 / math.sqrt(3.0)) * math.exp(-2 * q * (r / r0 - 1))
+    assert mb[1] == pytest.approx(want, rel=1e-14) and mb[0] == 0.0
+    with pytest.raises(gbmd.GbmdError):
+        gbmd.Plugin("gupta", "A 1 r0 2 p 3 B 4 q")  # a keyword without a value

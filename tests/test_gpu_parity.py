@@ -122,7 +122,7 @@ def test_fp64_trajectory(case):
         np.testing.assert_allclose(log[:, col], g["thermo"][:, col], rtol=1e-9, atol=1e-12)
 
 
-@pytest.mark.parametrize("case", ["lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo"])
+@pytest.mark.parametrize("case", ["lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au"])
 def test_mixed_forces_and_neighbors(case):
     g = load_golden(case)
     sim = make_sim(g, precision="mixed")

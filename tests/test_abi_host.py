@@ -136,5 +136,5 @@ def test_gupta_closed_form():
     mb = p.many_bodies([0.0, r, 0.0], 2.0, 3.0)
     want = (B * q / r0) * (1 / math.sqrt(2.0) + 1 / math.sqrt(3.0)) * math.exp(-2 * q * (r / r0 - 1))
     assert mb[1] == pytest.approx(want, rel=1e-14) and mb[0] == 0.0
-    with pytest.raises(gbmd.GbmdError):
+    with pytest.raises(SyntaxError, match="Unexpected end of input"):
         gbmd.Plugin("gupta", "A 1 r0 2 p 3 B 4 q")  # a keyword without a value

@@ -112,7 +112,8 @@ typedef struct gbmd_plugin gbmd_plugin;
  * PluginManager::LoadPlugin(name, id, args) + extern "C" create(std::string args) do
  * (liblpmd/plugins/pluginmanager.cc:123-143, liblpmd/lpmd/plugin.h:45-46).  Names:
  * "linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "gupta",
- * "finnissinclair", "finnissinclair-ext", "velocityverlet".  Arguments are parsed as
+ * "finnissinclair", "finnissinclair-ext", "velocityverlet", "euler", "leapfrog", "verlet",
+ * "beeman", "nosehoover".  Arguments are parsed as
  * Module::ProcessArguments does (liblpmd/plugins/module.cc:77-103): whitespace-separated
  * keyword/value pairs, a trailing keyword without a value is GBMD_ERR_SYNTAX. */
 gbmd_status gbmd_plugin_create(const char* name, const char* args, gbmd_plugin** out);

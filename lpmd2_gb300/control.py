@@ -11,7 +11,8 @@ simulation it describes through libgbmd:
   input module=lpmd|xyz file=F                                 first configuration of a file
   prepare temperature t=T [seed=S]                             velocities (see below)
   use linkedcell|verletlist|minimumimage|lennardjones|suttonchen|gupta|finnissinclair|
-      finnissinclair-ext|velocityverlet [as id] ... enduse     the timestep's plugins
+      finnissinclair-ext|velocityverlet|euler|leapfrog|verlet|
+      beeman|nosehoover [as id] ... enduse                     the timestep's plugins
   cellmanager <id> / potential <id> A B / integrator <id>      wiring (ids of use blocks)
   steps N                                                      velocity-Verlet steps
   monitor p1,p2,... [start= end= each= output=]                thermo columns (monitor.cc)
@@ -47,7 +48,7 @@ from . import formats as F
 from . import inputs as I
 
 TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "gupta", "finnissinclair",
-                    "finnissinclair-ext", "velocityverlet"}
+                    "finnissinclair-ext", "velocityverlet", "euler", "leapfrog", "verlet", "beeman", "nosehoover"}
 MODIFIER_PLUGINS = {"tempscaling", "temperature", "berendsen"}
 SKIPPED_STATEMENTS = {"property", "visualize", "filter", "average", "bond", "charge", "plugindir"}
 

@@ -203,12 +203,25 @@ PluginSpec make_plugin(const std::string& name, const std::string& args) {
       else if (pr == "fp64") p.precision = PREC_FP64;
       else throw Error(GBMD_ERR_PLUGIN, name + ": precision must be mixed or fp64");
     }
-  } else if (name == "velocityverlet") {
+  } else if (name == "velocityverlet" || name == "euler" || name == "leapfrog" || name == "verlet" ||
+             name == "beeman" || name == "nosehoover") {
+    // dt 1.0 and start 1 for all of them (plugins/velocityverlet.cc, euler.cc, leapfrog.cc,
+    // verlet.cc, beeman.cc); nosehoover adds fmass (no default) and t 300.0 (nosehoover.cc:13-24)
     p.kind = GBMD_KIND_INTEGRATOR;
     defaulted("dt", "1.0");
     defaulted("start", "1");
+    p.integ.kind = name == "velocityverlet" ? 0 : name == "euler" ? 1 : name == "leapfrog" ? 2
+                 : name == "verlet" ? 3 : name == "beeman" ? 4 : 5;
     p.integ.dt = num(p, "dt");
     p.integ.start = std::atol(p.get("start").c_str());
+    if (name == "nosehoover") {
+      defaulted("t", "300.0");
+      // an absent fmass reads as 0 in the reference and divides by zero: refused here
+      if (!has("fmass")) throw Error(GBMD_ERR_PLUGIN, "PluginError: nosehoover: the fmass keyword is required");
+      p.integ.fmass = num(p, "fmass");
+      p.integ.t = num(p, "t");
+      if (!(p.integ.fmass > 0.0)) throw Error(GBMD_ERR_PLUGIN, "PluginError: nosehoover: fmass must be positive");
+    }
   } else {
     throw Error(GBMD_ERR_PLUGIN, "PluginError: no GPU implementation of plugin \"" + name + "\"");
   }

@@ -46,6 +46,14 @@ constexpr int RING = 4;            // shared-memory stages of the list ring in t
 enum { PD_EPAIR = 0, PD_EEMBED = 1, PD_VIR = 2, PD_STRESS = 3, PD_KE = 12, PD_PX = 13 };
 // Per-system int64 fixed-point accumulators of the mixed path (atomics from every block)
 enum { SA_EPAIR = 0, SA_VIR = 1, SA_STRESS = 2, SA_KE = 11, SA_P = 12, SA_EEMBED = 15, SA_LEN = 16 };
+// Integrator history slots (each N doubles): the old position / velocity / acceleration an
+// integrator keeps (3), the previous old acceleration (3), the Nose-Hoover rank of the atom
+// among the atoms that move (1), and the positions and accelerations put aside while the
+// forces of the backed-up configuration are evaluated (3 + 3).
+enum { IS_OLD = 0, IS_AUX = 3, IS_RANK = 6, IS_SAVEX = 7, IS_SAVEA = 10, IST_K = 13 };
+// Nose-Hoover per-system record: friction after the last step, its increment per atom this
+// step, friction before this step, number of atoms that move.
+enum { NH_F = 0, NH_D = 1, NH_F0 = 2, NH_NMOVE = 3, NH_LEN = 4 };
 constexpr double FIX_KE = 17592186044416.0;  // 2^44: kinetic energy (amu A^2/fs^2) and momentum
 
 struct SysDev {
@@ -115,6 +123,12 @@ struct Dev {
   int list_blocks;
   // permutation scratch
   double* sdbl;   // 11*N doubles
+  // integrator history of the integrators other than velocityverlet (IST_K*N doubles, moved
+  // with the atoms when they are re-sorted; nullptr for velocityverlet), its re-sort scratch,
+  // and the Nose-Hoover friction per system (NH_LEN doubles each)
+  double* ist;
+  double* ist_alt;
+  double* nh;
   int* sint;      // 4*N ints
   unsigned char* sflags;
   // EAM

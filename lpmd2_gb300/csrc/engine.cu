@@ -12,6 +12,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "forces.cuh"
+#include "integrators.cuh"
 
 namespace gbmd {
 
@@ -749,8 +750,9 @@ struct Engine::Impl {
 
   // decide_next / cond_next: the mixed path's tail kernel also decides the next step's rebuild
   // and sets that step's graph conditional (0: a k_decide launch does it instead).
+  // raw: keep fixedvel atoms' accelerations (a bare UpdateForces outside an integrator step).
   void launch_force_passes(cudaStream_t s, int epi, int count_step, int decide_next = 0,
-                           cudaGraphConditionalHandle cond_next = 0) {
+                           cudaGraphConditionalHandle cond_next = 0, int raw = 0) {
     const bool mixed = precision == PREC_MIXED;
     const int np = (int)pots.size();
     mark_begin(s, T_FORCE);
@@ -771,6 +773,7 @@ struct Engine::Impl {
       sp.last = (p == np - 1);
       sp.count_step = count_step;
       sp.kinetic = 1;
+      sp.raw_acc = raw;
       const int mode = sysd[0].mode;
       if (P.kind != POT_LJ) {
         int first = (p == first_eam);
@@ -835,6 +838,14 @@ struct Engine::Impl {
   void ensure_ready() {
     if (!configured) configure();
     CK(cudaSetDevice(device));
+    if (integ.kind != INT_VV && !D.ist) {
+      // history of the integrators other than velocityverlet, moved with the atoms at re-sorts
+      D.ist = alloc<double>((size_t)IST_K * N);
+      D.ist_alt = alloc<double>((size_t)IST_K * N);
+      D.nh = alloc<double>((size_t)nsys * NH_LEN);
+      CK(cudaMemsetAsync(D.ist, 0, sizeof(double) * IST_K * N, stream));
+      CK(cudaMemsetAsync(D.nh, 0, sizeof(double) * nsys * NH_LEN, stream));
+    }
   }
 
   // Reads the per-system error words and the list statistics (synchronises the stream).
@@ -1027,11 +1038,145 @@ struct Engine::Impl {
   bool graph_cond = false;
   int64_t graph_launches = 0;  // kernels one graph launch runs, rebuild chains not included
 
+  // Integrator::Initialize of the integrators other than velocityverlet, at their first step
+  // (SimulationBuilder::DoStep, liblpmd/simulation/simulationbuilder.cc:130-133).
+  void init_integrator() {
+    const double dt = integ.dt;
+    const int k = integ.kind;
+    const unsigned nb = nblocks(N, 256);
+    set_buffers(cbuf);
+    if (k == INT_EULER) return;  // no Initialize of its own
+    if (k == INT_VERLET) {       // UseOldConfig: the backed-up positions; SetCellManager on the copy
+      k_init_backup<INT_VERLET><<<nb, 256, 0, stream>>>(D, dt);
+      launched();
+      pending_ucalls += 1;
+      return;
+    }
+    // leapfrog, beeman, nosehoover: UseOldConfig, then UpdateForces on the backed-up
+    // configuration (two UpdateCell calls), whose accelerations seed the history
+    if (k == INT_LEAPFROG)
+      k_init_backup<INT_LEAPFROG><<<nb, 256, 0, stream>>>(D, dt);
+    else
+      k_init_backup<INT_BEEMAN><<<nb, 256, 0, stream>>>(D, dt);
+    launched();
+    launch_decide(stream, 2 + pending_ucalls, 1, 0, 0);
+    pending_ucalls = 0;
+    launch_rebuild(stream);
+    launch_force_passes(stream, EPI_FORCES, 0, 0, 0, 1);
+    if (k == INT_LEAPFROG)
+      k_init_restore<INT_LEAPFROG><<<nb, 256, 0, stream>>>(D, dt);
+    else
+      k_init_restore<INT_BEEMAN><<<nb, 256, 0, stream>>>(D, dt);
+    k_force_rebuild<<<1, 256, 0, stream>>>(D);
+    launched(2);
+    check_launch("integrator initialize");
+    if (k == INT_NOSEHOOVER) init_nose_hoover();
+  }
+
+  // Nose-Hoover: friction 0 (nosehoover.cc:41), and each atom's rank among the atoms without
+  // fixedpos in the reference's atom order, which sets how many friction increments it sees.
+  void init_nose_hoover() {
+    std::vector<int> tag(N);
+    std::vector<unsigned char> fl(N, 0);
+    CK(cudaMemcpyAsync(tag.data(), D.tag, sizeof(int) * N, cudaMemcpyDeviceToHost, stream));
+    if (D.has_flags) CK(cudaMemcpyAsync(fl.data(), D.flags, N, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<double> rank_by_tag(N, 0.0), nh((size_t)nsys * NH_LEN, 0.0);
+    std::vector<unsigned char> fixed_by_tag(N, 0);
+    for (long long i = 0, s = 0; i < N; ++i) {
+      while (s + 1 < nsys && atom_base[s + 1] <= i) ++s;
+      fixed_by_tag[atom_base[s] + tag[i]] = (fl[i] & FLAG_FIXEDPOS) ? 1 : 0;
+    }
+    for (int s = 0; s < nsys; ++s) {
+      double r = 0.0;
+      for (long long t = 0; t < natoms[s]; ++t) {
+        if (!fixed_by_tag[atom_base[s] + t]) r += 1.0;
+        rank_by_tag[atom_base[s] + t] = r;
+      }
+      nh[(size_t)s * NH_LEN + NH_NMOVE] = r;
+    }
+    double* d_rank = nullptr;
+    CK(dev_malloc(&d_rank, sizeof(double) * std::max<long long>(N, 1)));
+    CK(cudaMemcpyAsync(d_rank, rank_by_tag.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(D.nh, nh.data(), sizeof(double) * nh.size(), cudaMemcpyHostToDevice, stream));
+    k_set_rank<<<nblocks(N, 256), 256, 0, stream>>>(D, d_rank);
+    launched();
+    CK(cudaStreamSynchronize(stream));
+    dev_free(d_rank);
+  }
+
+  // One step of an integrator other than velocityverlet (OneStepIntegrator::Advance /
+  // TwoStepIntegrator::Advance), then the step's thermo record from the new velocities.
+  void step_plain() {
+    const double dt = integ.dt;
+    const int k = integ.kind;
+    const bool mixed = precision == PREC_MIXED;
+    set_buffers(cbuf);
+    if (k == INT_EULER || k == INT_LEAPFROG || k == INT_VERLET) {
+      launch_decide(stream, 1 + pending_ucalls, 0, 0, 0);
+      pending_ucalls = 0;
+      launch_rebuild(stream);
+      launch_force_passes(stream, EPI_FORCES, 0);
+      if (k == INT_EULER)
+        k_onestep<INT_EULER><<<ntiles, TILE, 0, stream>>>(D, dt);
+      else if (k == INT_LEAPFROG)
+        k_onestep<INT_LEAPFROG><<<ntiles, TILE, 0, stream>>>(D, dt);
+      else
+        k_onestep<INT_VERLET><<<ntiles, TILE, 0, stream>>>(D, dt);
+      launched();
+      cbuf = 1 - cbuf;
+      set_buffers(cbuf);
+    } else {
+      // the step's first UpdateForces repeats the last evaluation at the same positions: only
+      // its UpdateCell call is counted
+      if (k == INT_NOSEHOOVER) {
+        k_kinetic_clear<<<1, 256, 0, stream>>>(D);
+        k_scale_kinetic<<<ntiles, TILE, 0, stream>>>(D, -1, 1);
+        k_nh_friction<<<1, 256, 0, stream>>>(D, dt, integ.fmass, integ.t);
+        k_twostep_position<INT_NOSEHOOVER><<<ntiles, TILE, 0, stream>>>(D, dt);
+        launched(4);
+      } else {
+        k_twostep_position<INT_BEEMAN><<<ntiles, TILE, 0, stream>>>(D, dt);
+        launched();
+      }
+      cbuf = 1 - cbuf;
+      set_buffers(cbuf);
+      launch_decide(stream, 2 + pending_ucalls, 0, 0, 0);
+      pending_ucalls = 0;
+      launch_rebuild(stream);
+      launch_force_passes(stream, EPI_FORCES, 0);
+      k_twostep_velocity<<<ntiles, TILE, 0, stream>>>(D, dt);
+      launched();
+    }
+    if (mixed) {
+      k_kinetic_slots_clear<<<1, 256, 0, stream>>>(D);
+      k_step_kinetic<1><<<ntiles, TILE, 0, stream>>>(D);
+      k_tail<<<1, 256, 0, stream>>>(D, 1, 0, 0ull);
+      launched(3);
+    } else {
+      k_step_kinetic<0><<<ntiles, TILE, 0, stream>>>(D);
+      k_thermo<<<nsys, TILE, 0, stream>>>(D, 1);
+      launched(2);
+    }
+    check_launch("step");
+  }
+
   void do_steps(int64_t nsteps) {
     ensure_ready();
     if (!have_integ) throw Error(4, "MissingComponent: integrator");
     if (nsteps <= 0) return;
     if (!forces_valid) update_forces();
+    if (integ.kind != INT_VV) {
+      if (!initialized) {
+        init_integrator();
+        initialized = true;
+      }
+      for (int64_t k = 0; k < nsteps; ++k) step_plain();
+      st.steps += nsteps;
+      st.force_evaluations += nsteps;
+      check_errors();
+      return;
+    }
     if (!pend) launch_drift(stream);
     int first_extra = 0;
     if (!initialized) {
@@ -1229,7 +1374,16 @@ void Engine::add_potential(const PotParams& p) {
 }
 
 void Engine::set_integrator(const IntegratorCfg& cfg) {
-  if (!(cfg.dt > 0.0) || !std::isfinite(cfg.dt)) throw Error(1, "velocityverlet: dt must be positive");
+  if (!(cfg.dt > 0.0) || !std::isfinite(cfg.dt)) throw Error(1, "integrator: dt must be positive");
+  if (cfg.kind < INT_VV || cfg.kind > INT_NOSEHOOVER) throw Error(1, "unknown integrator");
+  // A different integrator starts over with its own Initialize (its history is not the old
+  // one's) from forces at the current positions (a one-step integrator leaves the previous
+  // positions' accelerations).
+  if (d_->have_integ && cfg.kind != d_->integ.kind) {
+    d_->initialized = false;
+    d_->forces_valid = false;
+    d_->pend = false;
+  }
   d_->integ = cfg;
   d_->have_integ = true;
   d_->drop_graph();
@@ -1505,6 +1659,9 @@ static uint64_t config_hash(const Engine::Impl& I) {
   h = fnv_v(h, I.opt_skin);
   h = fnv_v(h, I.stencil_r);
   h = fnv_v(h, I.integ.dt);
+  h = fnv_v(h, I.integ.kind);
+  h = fnv_v(h, I.integ.fmass);
+  h = fnv_v(h, I.integ.t);
   for (const auto& P : I.pots) h = fnv(h, &P, sizeof(P));  // PotParams is zero-filled before use
   return h;
 }

@@ -55,8 +55,12 @@ struct CellManagerCfg {
 };
 
 struct IntegratorCfg {
+  int kind = 0;         // INT_* of integrators.cuh: 0 velocityverlet, 1 euler, 2 leapfrog, 3 verlet,
+                        // 4 beeman, 5 nosehoover
   double dt = 1.0;
   int64_t start = 1;
+  double fmass = 0.0;   // nosehoover: thermostat mass Q
+  double t = 300.0;     // nosehoover: target temperature
 };
 
 struct Thermo {

@@ -84,7 +84,7 @@ __device__ __forceinline__ float finish_atom(const Dev& D, const SysDev& S, long
   const double fm = MIXED ? D.fm[i] * (1.0 / FIX_F) : D.fm[i];
   double ax = dmul(Fx, fm), ay = dmul(Fy, fm), az = dmul(Fz, fm);
   unsigned char fl = D.has_flags ? D.flags[i] : 0;
-  if (fl & FLAG_FIXEDVEL) ax = ay = az = 0.0;
+  if ((fl & FLAG_FIXEDVEL) && !sp.raw_acc) ax = ay = az = 0.0;
   double vx = D.vx[i], vy = D.vy[i], vz = D.vz[i];
   if (sp.epi != EPI_FORCES && !(fl & FLAG_FIXEDPOS)) {
     if (MIXED) {

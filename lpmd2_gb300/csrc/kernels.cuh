@@ -38,6 +38,7 @@ struct StepParams {
   int last;             // last potential pass (write accelerations)
   int count_step;       // k_thermo advances the step counter
   int kinetic;          // compute kinetic sums in the epilogue
+  int raw_acc;          // keep fixedvel atoms' accelerations (a bare UpdateForces, no integrator)
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -234,6 +235,8 @@ __global__ void k_permute(Dev D) {
   si[1 * N + p] = D.tag[o];
   si[2 * N + p] = D.acell[o];
   if (D.has_flags) D.sflags[p] = D.flags[o];
+  if (D.ist)
+    for (int k = 0; k < IST_K; ++k) D.ist_alt[k * N + p] = D.ist[k * N + o];
 }
 
 // Offset of x from the centre xc of its home cell, wrapped into [-L/2, L/2).  Two FP64-pipe
@@ -306,6 +309,8 @@ __global__ void k_copyback(Dev D) {
   D.tag[p] = si[1 * N + p];
   D.home[p] = si[2 * N + p];
   if (D.has_flags) D.flags[p] = D.sflags[p];
+  if (D.ist)
+    for (int k = 0; k < IST_K; ++k) D.ist[k * N + p] = D.ist_alt[k * N + p];
   refresh_gather(D, D.sysd[s], p, true);
 }
 

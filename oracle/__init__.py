@@ -275,13 +275,19 @@ def _ref():
     return _REF
 
 
-def run_reference(pos, L, symbol, vel, cm, cm_args, pots, dt, nsteps, neigh=None):
+def run_reference(pos, L, symbol, vel, cm, cm_args, pots, dt, nsteps, neigh=None, integrator=None):
     """Runs the reference plugins (see ref_driver.cpp) and returns its outputs.
 
     pots: list of (name, args, s1, s2).  neigh: (full, rcut) to export neighbour lists after
-    the initial force evaluation.
+    the initial force evaluation.  integrator: (name, extra args) of the integrator plugin
+    (velocityverlet when None); "dt" is added.
     """
     lib = _ref()
+    if integrator is not None:
+        # these three need the runtime context supplied to the backed-up configuration (the
+        # unmodified reference throws MissingComponent at their first step; ref_driver.cpp)
+        supply = integrator[0] in ("leapfrog", "beeman", "nosehoover")
+        lib.ref_set_integrator(integrator[0].encode(), integrator[1].encode(), ctypes.c_int(int(supply)))
     n = len(pos)
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)

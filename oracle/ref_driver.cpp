@@ -27,7 +27,12 @@
 #include "linkedcell.h"
 #include "minimumimage.h"
 #include "suttonchen.h"
+#include "beeman.h"
+#include "euler.h"
+#include "leapfrog.h"
+#include "nosehoover.h"
 #include "velocityverlet.h"
+#include "verlet.h"
 #include "verletlist.h"
 
 #include <cstdint>
@@ -45,6 +50,18 @@ enum { T_STEP = 0, T_EPOT, T_EKIN, T_ETOT, T_TEMP, T_VIRIAL, T_PX, T_PY, T_PZ, T
        T_VIRIAL_PRESSURE, T_KINETIC_PRESSURE, T_PRESSURE, T_STRESS, THERMO_LEN = 22 };
 
 char g_error[512];
+std::string g_integ_name = "velocityverlet", g_integ_args;  // integrator of the next ref_run
+bool g_supply_context = false;  // give the backed-up configuration the runtime context
+
+Integrator* make_integ(const std::string& name, const std::string& args) {
+  if (name == "velocityverlet") return new VelocityVerlet(args);
+  if (name == "euler") return new Euler(args);
+  if (name == "leapfrog") return new Leapfrog(args);
+  if (name == "verlet") return new Verlet(args);
+  if (name == "beeman") return new Beeman(args);
+  if (name == "nosehoover") return new NoseHoover(args);
+  return nullptr;
+}
 
 CellManager* make_cm(const std::string& name, const std::string& args) {
   if (name == "linkedcell") return new LinkedCell(args);
@@ -107,6 +124,14 @@ void neighbors(Simulation& md, int full, double rcut, int64_t* counts, int64_t* 
 
 extern "C" const char* ref_last_error() { return g_error; }
 
+// Selects the integrator plugin (and its arguments, "dt" appended by ref_run) of the next
+// ref_run call, velocityverlet afterwards; supply_context: see ref_run.
+extern "C" void ref_set_integrator(const char* name, const char* args, int supply_context) {
+  g_integ_name = name ? name : "velocityverlet";
+  g_integ_args = args ? args : "";
+  g_supply_context = supply_context != 0;
+}
+
 // Runs one reference simulation.  Inputs are xyz-interleaved.  Outputs (each may be NULL):
 //   out_mass[n]                     masses the reference assigned from `symbol`
 //   out_acc0[3n], out_thermo0[22]   after the initial Potentials().UpdateForces(md)
@@ -153,11 +178,17 @@ extern "C" int ref_run(int64_t n, const double* L, const char* symbol, const dou
       pot->SetValidSpecies(spc[2 * p], spc[2 * p + 1]);
       md.Potentials().Append(*pot);
     }
-    VelocityVerlet* vv = nullptr;
+    Integrator* vv = nullptr;
     if (nsteps > 0) {
       char dtarg[64];
       std::snprintf(dtarg, sizeof dtarg, "dt %.17g", dt);
-      vv = new VelocityVerlet(dtarg);
+      vv = make_integ(g_integ_name, std::string(dtarg) + (g_integ_args.empty() ? "" : " " + g_integ_args));
+      g_integ_name = "velocityverlet";
+      g_integ_args.clear();
+      if (!vv) {
+        std::snprintf(g_error, sizeof g_error, "unknown integrator");
+        return 1;
+      }
       md.SetIntegrator(*vv);
     }
     md.Potentials().Initialize(md);
@@ -168,6 +199,16 @@ extern "C" int ref_run(int64_t n, const double* L, const char* symbol, const dou
     if (out_thermo0) thermo(md, out_thermo0);
     if (neigh_counts || neigh_idx || neigh_total)
       neighbors(md, neigh_full, neigh_rcut, neigh_counts, neigh_idx, neigh_cap, neigh_total);
+    if (vv && g_supply_context) {
+      // leapfrog / beeman / nosehoover: Initialize evaluates forces on the configuration
+      // UseOldConfig backs up, which never receives the runtime context, so the unmodified
+      // reference throws MissingComponent("runtime_context") at its first step.  The backup is
+      // made here, where Initialize would make it, and given the context; Initialize then
+      // finds it and runs the reference's own code unchanged.
+      vv->UseOldConfig(md);
+      vv->OldConfig().SetRuntimeContext(context);
+    }
+    g_supply_context = false;
     for (int64_t k = 0; k < nsteps; ++k) {
       md.DoStep();
       if (out_thermo) thermo(md, out_thermo + k * THERMO_LEN);

@@ -28,13 +28,13 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
 import oracle  # noqa: E402
-from helpers import GOLDEN, GOLDEN_CASES, neighbor_hashes, workload  # noqa: E402
+from helpers import GOLDEN, GOLDEN_CASES, INTEG_CASES, neighbor_hashes, workload  # noqa: E402
 
 
 def make(name: str) -> None:
     w = workload(name)
     out = oracle.run_reference(w["pos"], w["L"], w["symbol"], w["vel"], w["cm"], w["cm_args"],
-                               w["pots"], w["dt"], w["nsteps"], neigh=w["neigh"])
+                               w["pots"], w["dt"], w["nsteps"], neigh=w["neigh"], integrator=w.get("integ"))
     n = len(w["pos"])
     rec = dict(
         pos_in=w["pos"], vel_in=w["vel"], L=w["L"], Z=np.full(n, w["Z"], dtype=np.int32),
@@ -56,6 +56,9 @@ def make(name: str) -> None:
     rec["pot_names"] = np.array([p[0] for p in w["pots"]])
     rec["pot_args"] = np.array([p[1] for p in w["pots"]])
     rec["pot_species"] = np.array([[p[2], p[3]] for p in w["pots"]], dtype=np.int32)
+    integ = w.get("integ", ("velocityverlet", ""))
+    rec["integ_name"] = np.array(integ[0])
+    rec["integ_args"] = np.array(integ[1])
     np.savez_compressed(GOLDEN / f"{name}.npz", **rec)
     print(f"{name}: N={n} E0={out['thermo0'][1]:.10f} steps={w['nsteps']}")
 
@@ -63,5 +66,5 @@ def make(name: str) -> None:
 if __name__ == "__main__":
     if not oracle.reference_available():
         oracle.build()
-    for case in sys.argv[1:] or GOLDEN_CASES:
+    for case in sys.argv[1:] or GOLDEN_CASES + INTEG_CASES:
         make(case)

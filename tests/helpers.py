@@ -96,6 +96,23 @@ def workload(name: str) -> dict:
         return dict(pos=pos, L=L, symbol="Au", Z=79, vel=I.maxwell_boltzmann(m, 400.0, seed=8),
                     cm="linkedcell", cm_args="cutoff 6.0 nx 4 ny 4 nz 4",
                     pots=[("gupta", GUPTA_AU, -1, -1)], dt=2.0, nsteps=20, neigh=(1, 6.0))
+    if name.startswith("lj_integ_"):
+        # the same argon liquid under each integrator other than velocityverlet
+        kind = name[len("lj_integ_"):]
+        s_ = I.lj_system(5, 0.8, 1.2, seed=21)
+        integ = (kind, "fmass 2e9 t 120.0" if kind == "nosehoover" else "")
+        return dict(pos=s_["pos"], L=s_["L"], symbol="Ar", Z=18, vel=s_["vel"], cm="linkedcell",
+                    cm_args="cutoff 8.5 nx 3 ny 3 nz 3", pots=[("lennardjones", LJ_AR, -1, -1)], dt=2.0,
+                    nsteps=30, neigh=(1, 8.5), integ=integ)
+    if name == "sc_integ_beeman":
+        # three cells per axis: with two, the reference's LinkedCell stencil visits a cell twice
+        pos, L = I.fcc_fast(6, 6, 6, 3.61)
+        pos = I.remove_sites(pos, 0.01, seed=23)
+        m = np.full(len(pos), I.MASSES["Cu"])
+        return dict(pos=pos, L=L, symbol="Cu", Z=29, vel=I.maxwell_boltzmann(m, 600.0, seed=23),
+                    cm="linkedcell", cm_args="cutoff 7.22 nx 3 ny 3 nz 3",
+                    pots=[("suttonchen", SC_CU, -1, -1)], dt=2.0, nsteps=20, neigh=(1, 7.22),
+                    integ=("beeman", ""))
     if name == "lj_auto":
         pos, L = I.fcc_crystal3d(10, 10, 10, 5.26)
         m = np.full(len(pos), I.MASSES["Ar"])
@@ -112,6 +129,9 @@ def workload(name: str) -> dict:
 
 
 GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_auto", "lj_nx2"]
+# integrators other than velocityverlet (fixtures from the reference's own plugins)
+INTEG_CASES = ["lj_integ_euler", "lj_integ_leapfrog", "lj_integ_verlet", "lj_integ_beeman", "lj_integ_nosehoover",
+               "sc_integ_beeman"]
 
 
 def load_golden(name: str) -> dict:

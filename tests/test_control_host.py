@@ -44,13 +44,13 @@ def test_parse_statements_and_blocks():
     assert ctl.steps == 2000
     assert ctl.uses["lennardjones"] == ("lennardjones", "sigma 3.41 epsilon 0.0103408 cutoff 8.5")
     assert ctl.uses["vv"] == ("velocityverlet", "dt 1.0")
-    assert "integ" not in ctl.uses  # beeman is not on the GPU path
+    assert ctl.uses["integ"] == ("beeman", "dt 1.0")  # declared; the integrator statement picks vv
     assert ctl.cellmanager == "minimumimage" and ctl.integrator == "vv"
     assert ctl.potentials == [("lennardjones", "Ar", "Ar")]
     assert ctl.monitors == [{"properties": "step,total-energy,temperature", "start": "0", "end": "-1", "each": "100"}]
     assert ctl.outputs == [{"module": "xyz", "file": "frames.xyz", "each": "10"}]
     assert ctl.prepares == [{"module": "temperature", "t": "10.0"}]
-    assert ctl.skipped == ["use beeman", "use gdr", "property gdr each=100"]
+    assert ctl.skipped == ["use gdr", "property gdr each=100"]
 
 
 def test_strict_rejects_modules_off_the_path():

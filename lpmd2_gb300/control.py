@@ -47,7 +47,8 @@ import numpy as np
 from . import formats as F
 from . import inputs as I
 
-TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "suttonchen", "gupta", "finnissinclair",
+TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "fastlj", "suttonchen", "gupta",
+                    "finnissinclair",
                     "finnissinclair-ext", "velocityverlet", "euler", "leapfrog", "verlet", "beeman", "nosehoover"}
 MODIFIER_PLUGINS = {"tempscaling", "temperature", "berendsen"}
 SKIPPED_STATEMENTS = {"property", "visualize", "filter", "average", "bond", "charge", "plugindir"}

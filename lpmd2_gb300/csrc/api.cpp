@@ -73,9 +73,12 @@ PotParams finalize_potential(int kind, const double* v, int s1, int s2) {
   P.kind = kind;
   P.spc_sum = s1 + s2;
   P.int_n = P.int_m = -1;
-  int np = (kind == POT_LJ) ? 3 : (kind == POT_SC || kind == POT_GUPTA) ? 6 : (kind == POT_FS) ? 7 : 9;
+  int np = (kind == POT_LJ) ? 3 : (kind == POT_FASTLJ) ? 4 : (kind == POT_SC || kind == POT_GUPTA) ? 6
+         : (kind == POT_FS) ? 7 : 9;
   for (int k = 0; k < np; ++k) P.p[k] = v[k];
-  if (kind == POT_LJ) {
+  if (kind == POT_FASTLJ) {
+    P.cutoff = v[2];  // plugins/fastlj.cc:24; v[3] = bins (FP64 only: no mixed constants)
+  } else if (kind == POT_LJ) {
     P.cutoff = v[2];
     const double s = v[0], e = v[1];
     P.f[0] = (float)(s * s);
@@ -182,17 +185,21 @@ PluginSpec make_plugin(const std::string& name, const std::string& args) {
     p.cm.kind = CM_MINIMUMIMAGE;
     p.cm.cutoff = num(p, "cutoff");
   } else if (name == "lennardjones" || name == "suttonchen" || name == "finnissinclair" ||
-             name == "finnissinclair-ext" || name == "gupta") {
+             name == "finnissinclair-ext" || name == "gupta" || name == "fastlj") {
     p.kind = GBMD_KIND_POTENTIAL;
     static const char* lj[] = {"sigma", "epsilon", "cutoff"};
     static const char* sc[] = {"e", "a", "n", "m", "c", "cutoff"};
     static const char* fs[] = {"c0", "c1", "c2", "A", "B", "c", "d"};
     static const char* fx[] = {"c0", "c1", "c2", "c3", "c4", "A", "B", "c", "d"};
     static const char* gu[] = {"A", "r0", "p", "B", "q", "cutoff"};  // plugins/gupta.cc:14-19
+    static const char* fl[] = {"sigma", "epsilon", "cutoff", "bins"};  // plugins/fastlj.cc:15-19
     int kind = name == "lennardjones" ? POT_LJ : name == "suttonchen" ? POT_SC : name == "finnissinclair" ? POT_FS
-             : name == "gupta" ? POT_GUPTA : POT_FSEXT;
-    const char** keys = kind == POT_LJ ? lj : kind == POT_SC ? sc : kind == POT_FS ? fs : kind == POT_GUPTA ? gu : fx;
-    int nk = kind == POT_LJ ? 3 : (kind == POT_SC || kind == POT_GUPTA) ? 6 : kind == POT_FS ? 7 : 9;
+             : name == "gupta" ? POT_GUPTA : name == "fastlj" ? POT_FASTLJ : POT_FSEXT;
+    const char** keys = kind == POT_LJ ? lj : kind == POT_SC ? sc : kind == POT_FS ? fs : kind == POT_GUPTA ? gu
+                      : kind == POT_FASTLJ ? fl : fx;
+    int nk = kind == POT_LJ ? 3 : kind == POT_FASTLJ ? 4 : (kind == POT_SC || kind == POT_GUPTA) ? 6
+           : kind == POT_FS ? 7 : 9;
+    if (kind == POT_FASTLJ) defaulted("bins", "500");
     if (kind == POT_SC) defaulted("corrections", "false");
     double v[10] = {0};
     for (int k = 0; k < nk; ++k) v[k] = num(p, keys[k]);
@@ -232,6 +239,24 @@ PluginSpec make_plugin(const std::string& name, const std::string& args) {
 // Host FP64 functionals, evaluated exactly as the reference plugins write them.
 void potential_eval(const PotParams& P, int what, const double* a, double* out) {
   const double* v = P.p;
+  if (P.kind == POT_FASTLJ) {  // plugins/fastlj.cc:38-73: the table entry of the distance's bin
+    const double sigma = v[0], epsilon = v[1], cutoff = v[2];
+    const long bins = (long)v[3];
+    double r = what == 0 ? a[0] : std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    long k = long(std::floor(bins * r / cutoff));
+    if (what > 1) throw Error(GBMD_ERR_INVALID, "fastlj is a pair potential: only pairEnergy and pairForce");
+    if (k < 0 || k >= bins) throw Error(GBMD_ERR_INVALID, "fastlj: distance outside the table");
+    double rk = cutoff * double(k) / double(bins);
+    double r6 = std::pow(sigma / rk, 6.0e0);
+    double r12 = r6 * r6;
+    if (what == 0) {
+      out[0] = 4.0e0 * epsilon * (r12 - r6);
+    } else {
+      double ff = -48.0e0 * (epsilon / (rk * rk)) * (r12 - 0.50e0 * r6);
+      for (int q = 0; q < 3; ++q) out[q] = a[q] * ff;
+    }
+    return;
+  }
   if (P.kind == POT_LJ) {
     const double sigma = v[0], epsilon = v[1];
     if (what == 0) {  // plugins/lennardjones.cc:53-58

@@ -223,6 +223,23 @@ __global__ void k_clear_state(Dev D, int nsys) {
 // Engine implementation
 // ------------------------------------------------------------------------------------------
 
+// Pair potentials (LennardJones, FastLJ) run the pair kernels; the rest are metal potentials.
+inline bool pair_kind(int k) { return k == POT_LJ || k == POT_FASTLJ; }
+
+// FastLJ::Tabulate (plugins/fastlj.cc:38-54): LJ at the lower edge r = cutoff i / bins of every
+// bin, energies then force factors.
+static std::vector<double> fastlj_table(double sigma, double epsilon, double cutoff, long bins) {
+  std::vector<double> t(2 * (size_t)bins);
+  for (long i = 0; i < bins; ++i) {
+    double r = cutoff * double(i) / double(bins);
+    double r6 = std::pow(sigma / r, 6.0e0);
+    double r12 = r6 * r6;
+    t[i] = 4.0e0 * epsilon * (r12 - r6);
+    t[bins + i] = -48.0e0 * (epsilon / (r * r)) * (r12 - 0.50e0 * r6);
+  }
+  return t;
+}
+
 struct Engine::Impl {
   int device = 0;
   cudaStream_t stream = nullptr, stream2 = nullptr;
@@ -758,7 +775,7 @@ struct Engine::Impl {
     mark_begin(s, T_FORCE);
     int first_eam = -1;
     for (int p = 0; p < np; ++p)
-      if (pots[p].kind != POT_LJ) {
+      if (!pair_kind(pots[p].kind)) {
         first_eam = p;
         break;
       }
@@ -775,7 +792,7 @@ struct Engine::Impl {
       sp.kinetic = 1;
       sp.raw_acc = raw;
       const int mode = sysd[0].mode;
-      if (P.kind != POT_LJ) {
+      if (!pair_kind(P.kind)) {
         int first = (p == first_eam);
         if (mixed && P.kind == POT_SC && P.int_m == 6)
           k_eam_density32<6><<<ntiles, TILE, 0, s>>>(D, P);
@@ -791,7 +808,7 @@ struct Engine::Impl {
       }
       if (mixed) {
         const bool species = P.spc_sum >= 0;
-        if (P.kind == POT_LJ) {
+        if (pair_kind(P.kind)) {
           if (species)
             k_force32<PC_PAIR, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
           else
@@ -810,17 +827,17 @@ struct Engine::Impl {
             k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
         }
       } else if (mode == NB_LIST) {
-        if (P.kind == POT_LJ)
+        if (pair_kind(P.kind))
           k_force64<NB_LIST, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
         else
           k_force64<NB_LIST, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
       } else if (mode == NB_CELLS) {
-        if (P.kind == POT_LJ)
+        if (pair_kind(P.kind))
           k_force64<NB_CELLS, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
         else
           k_force64<NB_CELLS, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
       } else {
-        if (P.kind == POT_LJ)
+        if (pair_kind(P.kind))
           k_force64<NB_ALLPAIRS, PC_PAIR><<<ntiles, TILE, 0, s>>>(D, P, sp);
         else
           k_force64<NB_ALLPAIRS, PC_EAM><<<ntiles, TILE, 0, s>>>(D, P, sp);
@@ -836,6 +853,10 @@ struct Engine::Impl {
   }
 
   void ensure_ready() {
+    for (const auto& P : pots)
+      if (P.kind == POT_FASTLJ && precision == PREC_MIXED)
+        throw Error(1, "fastlj has no mixed-precision form (an FP32 distance can fall into the neighbouring "
+                       "table bin): use precision fp64");
     if (!configured) configure();
     CK(cudaSetDevice(device));
     if (integ.kind != INT_VV && !D.ist) {
@@ -1367,7 +1388,18 @@ void Engine::set_cell_manager(const CellManagerCfg& cfg) {
 
 void Engine::add_potential(const PotParams& p) {
   if (d_->pots.size() >= 8) throw Error(1, "at most 8 potentials");
-  d_->pots.push_back(p);
+  PotParams q = p;
+  q.tab = nullptr;
+  if (p.kind == POT_FASTLJ) {
+    const long bins = (long)p.p[3];
+    if (bins < 1 || bins > (1L << 24)) throw Error(1, "fastlj: bins must be in [1, 2^24]");
+    std::vector<double> t = fastlj_table(p.p[0], p.p[1], p.p[2], bins);
+    CK(cudaSetDevice(d_->device));
+    double* d = d_->alloc<double>(t.size());
+    CK(cudaMemcpy(d, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice));
+    q.tab = d;
+  }
+  d_->pots.push_back(q);
   d_->configured = false;
   d_->forces_valid = false;
   d_->forces_valid_layout = false;
@@ -1662,7 +1694,10 @@ static uint64_t config_hash(const Engine::Impl& I) {
   h = fnv_v(h, I.integ.kind);
   h = fnv_v(h, I.integ.fmass);
   h = fnv_v(h, I.integ.t);
-  for (const auto& P : I.pots) h = fnv(h, &P, sizeof(P));  // PotParams is zero-filled before use
+  for (auto P : I.pots) {  // PotParams is zero-filled before use; the table pointer is this engine's own
+    P.tab = nullptr;
+    h = fnv(h, &P, sizeof(P));
+  }
   return h;
 }
 

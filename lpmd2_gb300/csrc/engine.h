@@ -7,7 +7,7 @@
 //                           liblpmd/simulation/simulationbuilder.cc:126-136,
 //                           liblpmd/simulation/twostepintegrator.cc:12-68
 //   CellManagerCfg          LinkedCell / VerletListCellManager / MinimumImage plugins
-//   PotParams               LennardJones / SuttonChen / FinnisSinclair(-Ext) / Gupta plugins
+//   PotParams               LennardJones / FastLJ / SuttonChen / FinnisSinclair(-Ext) / Gupta plugins
 #pragma once
 
 #include <array>
@@ -24,7 +24,7 @@ struct Error : std::runtime_error {
   Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
 
-enum PotKind { POT_LJ = 1, POT_SC = 2, POT_FS = 3, POT_FSEXT = 4, POT_GUPTA = 5 };
+enum PotKind { POT_LJ = 1, POT_SC = 2, POT_FS = 3, POT_FSEXT = 4, POT_GUPTA = 5, POT_FASTLJ = 6 };
 enum CmKind { CM_LINKEDCELL = 1, CM_VERLETLIST = 2, CM_MINIMUMIMAGE = 3 };
 enum NbMode { NB_ALLPAIRS = 0, NB_CELLS = 1, NB_LIST = 2 };
 enum Rebuild { REBUILD_SKIN = 0, REBUILD_EACH = 1, REBUILD_BOTH = 2 };
@@ -40,6 +40,7 @@ struct PotParams {
   double an, am;      // Sutton-Chen pow(a, n), pow(a, m)
   int int_n, int_m;   // integral Sutton-Chen exponents (or -1: general pow)
   float f[16];        // FP32 constants of the mixed path
+  const double* tab;  // fastlj: device tables etable[bins], fftable[bins] (set by add_potential)
 };
 
 struct CellManagerCfg {

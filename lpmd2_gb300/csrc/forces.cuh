@@ -153,7 +153,10 @@ __global__ void __launch_bounds__(TILE) k_force64(Dev D, PotParams P, StepParams
       if (r2 < P.rc2 && applies_to(P.spc_sum, ti, (int)pj.w)) {
         double g, e;
         if (PC == PC_PAIR) {
-          lj_pair64(P, r2, g, e);
+          if (P.kind == POT_FASTLJ)
+            fastlj_pair64(P, r2, g, e);
+          else
+            lj_pair64(P, r2, g, e);
         } else {
           double r = sqrt(r2);
           double sc;

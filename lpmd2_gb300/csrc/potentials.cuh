@@ -53,6 +53,17 @@ __device__ __forceinline__ void lj_pair64(const PotParams& P, double r2, double&
   e = dmul(dmul(4.0, eps), dsub(r12, r6));
 }
 
+// FastLJ pairEnergy / pairForce (plugins/fastlj.cc:56-73): the tabulated LJ values of bin
+// k = floor(bins r / cutoff) (no interpolation).  k is clamped to the last bin, which a distance
+// that rounds to the cutoff would otherwise pass (the reference reads past its table there).
+__device__ __forceinline__ void fastlj_pair64(const PotParams& P, double r2, double& g, double& e) {
+  const long bins = (long)P.p[3];
+  long k = (long)floor(ddiv(dmul((double)bins, sqrt(r2)), P.cutoff));
+  if (k > bins - 1) k = bins - 1;
+  e = P.tab[k];
+  g = P.tab[bins + k];
+}
+
 // rhoij(r) for the EAM density pass.
 __device__ __forceinline__ double eam_rho64(const PotParams& P, double r) {
   if (P.kind == POT_GUPTA) {  // plugins/gupta.cc:56: exp(-2 q (r - r0) / r0)

@@ -20,13 +20,15 @@ THERMO_FIELDS = ["step", "epot", "ekin", "etot", "temperature", "virial", "px", 
                  "volume", "virial_pressure", "kinetic_pressure", "pressure"]
 
 CM_KIND = {"linkedcell": 1, "verletlist": 2, "minimumimage": 3}
-POT_KIND = {"lennardjones": 1, "suttonchen": 2, "finnissinclair": 3, "finnissinclair-ext": 4, "gupta": 5}
+POT_KIND = {"lennardjones": 1, "suttonchen": 2, "finnissinclair": 3, "finnissinclair-ext": 4, "gupta": 5,
+            "fastlj": 6}
 POT_KEYS = {
     "lennardjones": ["sigma", "epsilon", "cutoff"],
     "suttonchen": ["e", "a", "n", "m", "c", "cutoff"],
     "finnissinclair": ["c0", "c1", "c2", "A", "B", "c", "d"],
     "finnissinclair-ext": ["c0", "c1", "c2", "c3", "c4", "A", "B", "c", "d"],
     "gupta": ["A", "r0", "p", "B", "q", "cutoff"],
+    "fastlj": ["sigma", "epsilon", "cutoff", "bins"],
 }
 ERRORS = {1: "invalid argument", 2: "maxneighbors is too small!", 3: "out of memory",
           4: "missing component", 5: "capacity"}
@@ -155,7 +157,8 @@ class PortSim:
 
     def add_potential(self, name: str, args: str, s1: int = -1, s2: int = -1):
         kw = parse_args(args)
-        p = np.array([float(kw.get(k, 0.0)) for k in POT_KEYS[name]], dtype=np.float64)
+        defaults = {"bins": 500.0} if name == "fastlj" else {}  # plugins/fastlj.cc:19
+        p = np.array([float(kw.get(k, defaults.get(k, 0.0))) for k in POT_KEYS[name]], dtype=np.float64)
         _check(self.lib.orc_sim_add_potential(self.h, POT_KIND[name], _ptr(p), len(p), s1, s2))
 
     def set_integrator(self, dt: float):

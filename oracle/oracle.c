@@ -30,6 +30,9 @@ typedef struct {
   double an, am;
   /* MetalPotential state: the per-atom density of the last force call */
   double* rho;
+  /* FastLJ tables: etable[bins], fftable[bins] */
+  double* tab;
+  long bins;
 } orc_pot;
 
 typedef struct {
@@ -487,6 +490,35 @@ static double lj_energy(const orc_pot* p, double r) {
   return 4.0e0 * epsilon * (r12 - r6);
 }
 
+/* FastLJ::Tabulate, plugins/fastlj.cc:38-54: LJ at the lower edge of every bin. */
+static int fastlj_tabulate(orc_pot* p) {
+  const double sigma = p->p[0], epsilon = p->p[1], cutoff = p->p[2];
+  p->tab = (double*)malloc(sizeof(double) * 2 * (size_t)p->bins);
+  if (!p->tab)
+    return ORC_ERR_NOMEM;
+  for (long i = 0; i < p->bins; ++i) {
+    double r = cutoff * (double)i / (double)p->bins;
+    double r6 = pow(sigma / r, 6.0e0);
+    double r12 = r6 * r6;
+    p->tab[i] = 4.0e0 * epsilon * (r12 - r6);
+    p->tab[p->bins + i] = -48.0e0 * (epsilon / (r * r)) * (r12 - 0.50e0 * r6);
+  }
+  return ORC_OK;
+}
+
+/* FastLJ::pairEnergy / pairForce, plugins/fastlj.cc:56-73: the bin floor(bins r / cutoff). */
+static long fastlj_bin(const orc_pot* p, double r) { return (long)floor(p->bins * r / p->cutoff); }
+
+static double fastlj_energy(const orc_pot* p, double r) { return p->tab[fastlj_bin(p, r)]; }
+
+static void fastlj_force(const orc_pot* p, const double r[3], double out[3]) {
+  double rr = sqrt(sqmod(r));
+  double ff = p->tab[p->bins + fastlj_bin(p, rr)];
+  out[0] = r[0] * ff;
+  out[1] = r[1] * ff;
+  out[2] = r[2] * ff;
+}
+
 /* LennardJones::pairForce, plugins/lennardjones.cc:60-67. */
 static void lj_force(const orc_pot* p, const double r[3], double out[3]) {
   const double sigma = p->p[0], epsilon = p->p[1];
@@ -655,9 +687,14 @@ static int pair_update_forces(orc_sim* s, int pi) {
       const double* rij = &s->lrij[3 * k];
       double r2 = s->lr2[k];
       if (applies_to(p, s->Z[i], s->Z[j]) && r2 < cutoff * cutoff) {
-        etmp += lj_energy(p, sqrt(r2));
         double ff[3];
-        lj_force(p, rij, ff);
+        if (p->kind == ORC_POT_FASTLJ) {
+          etmp += fastlj_energy(p, sqrt(r2));
+          fastlj_force(p, rij, ff);
+        } else {
+          etmp += lj_energy(p, sqrt(r2));
+          lj_force(p, rij, ff);
+        }
         double fi = (forcefactor / s->mass[i]);
         double fj = (forcefactor / s->mass[j]);
         for (int q = 0; q < 3; ++q)
@@ -799,8 +836,10 @@ void orc_sim_destroy(orc_sim* s) {
   free(s->Z);
   free(s->mass);
   free(s->flags);
-  for (int i = 0; i < s->npots; ++i)
+  for (int i = 0; i < s->npots; ++i) {
     free(s->pots[i].rho);
+    free(s->pots[i].tab);
+  }
   cm_free(s->cm);
   free(s->lj);
   free(s->lrij);
@@ -900,8 +939,9 @@ int orc_sim_set_minimumimage(orc_sim* s, double cutoff) {
 int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparams, int s1, int s2) {
   if (s->npots >= ORC_MAXPOT)
     return ORC_ERR_INVALID;
-  int need = (kind == ORC_POT_LJ) ? 3 : (kind == ORC_POT_SC || kind == ORC_POT_GUPTA) ? 6 : (kind == ORC_POT_FS) ? 7 : 9;
-  if (kind < ORC_POT_LJ || kind > ORC_POT_GUPTA || nparams < need)
+  int need = (kind == ORC_POT_LJ) ? 3 : (kind == ORC_POT_FASTLJ) ? 4
+           : (kind == ORC_POT_SC || kind == ORC_POT_GUPTA) ? 6 : (kind == ORC_POT_FS) ? 7 : 9;
+  if (kind < ORC_POT_LJ || kind > ORC_POT_FASTLJ || nparams < need)
     return ORC_ERR_INVALID;
   orc_pot* p = &s->pots[s->npots];
   memset(p, 0, sizeof(*p));
@@ -917,6 +957,13 @@ int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparam
     p->am = pow(params[1], params[3]);
   } else if (kind == ORC_POT_GUPTA) {
     p->cutoff = params[5]; /* gupta.cc:26 */
+  } else if (kind == ORC_POT_FASTLJ) {
+    p->cutoff = params[2]; /* fastlj.cc:24 */
+    p->bins = (long)params[3];
+    if (p->bins < 1)
+      return ORC_ERR_INVALID;
+    if (fastlj_tabulate(p) != ORC_OK)
+      return ORC_ERR_NOMEM;
   } else if (kind == ORC_POT_FS) {
     double c = params[5], d = params[6];
     p->cutoff = (d >= c) ? d : c; /* finnissinclair.cc:27-30 */
@@ -946,7 +993,8 @@ int orc_sim_update_forces(orc_sim* s) {
   if (e)
     return e;
   for (int p = 0; p < s->npots; ++p) {
-    e = (s->pots[p].kind == ORC_POT_LJ) ? pair_update_forces(s, p) : metal_update_forces(s, p);
+    e = (s->pots[p].kind == ORC_POT_LJ || s->pots[p].kind == ORC_POT_FASTLJ) ? pair_update_forces(s, p)
+                                                                             : metal_update_forces(s, p);
     if (e)
       return e;
   }

@@ -18,6 +18,7 @@
  *   - FinnisSinclair / FinnisSinclairExt             plugins/finnissinclair.cc:75-113,
  *                                                    plugins/finnissinclair-ext.cc:85-128
  *   - Gupta functionals                              plugins/gupta.cc:52-75
+ *   - FastLJ tables and lookups                      plugins/fastlj.cc:38-73
  *   - CombinedPotential::UpdateForces                liblpmd/lpmd/combinedpotential.h:39-52
  *   - TwoStepIntegrator::Advance + VelocityVerlet    liblpmd/simulation/twostepintegrator.cc:12-68,
  *                                                    plugins/velocityverlet.cc:55-75,
@@ -54,7 +55,7 @@ enum {
 
 enum { ORC_CM_LINKEDCELL = 1, ORC_CM_VERLETLIST = 2, ORC_CM_MINIMUMIMAGE = 3 };
 
-enum { ORC_POT_LJ = 1, ORC_POT_SC = 2, ORC_POT_FS = 3, ORC_POT_FSEXT = 4, ORC_POT_GUPTA = 5 };
+enum { ORC_POT_LJ = 1, ORC_POT_SC = 2, ORC_POT_FS = 3, ORC_POT_FSEXT = 4, ORC_POT_GUPTA = 5, ORC_POT_FASTLJ = 6 };
 
 /* Per-atom flag bits, standing in for the "fixedvel" / "fixedpos" atom tags
  * (liblpmd/simulation/twostepintegrator.cc:20-41). */

@@ -21,6 +21,7 @@
 #include "finnissinclair-ext.h"
 #include "lpmd.h"
 #include "xyz.h"
+#include "fastlj.h"
 #include "finnissinclair.h"
 #include "gupta.h"
 #include "lennardjones.h"
@@ -76,6 +77,7 @@ Potential* make_pot(const std::string& name, const std::string& args) {
   if (name == "finnissinclair") return new FinnisSinclair(args);
   if (name == "finnissinclair-ext") return new FinnisSinclairExt(args);
   if (name == "gupta") return new Gupta(args);
+  if (name == "fastlj") return new FastLJ(args);
   return nullptr;
 }
 

@@ -113,6 +113,11 @@ def workload(name: str) -> dict:
                     cm="linkedcell", cm_args="cutoff 7.22 nx 3 ny 3 nz 3",
                     pots=[("suttonchen", SC_CU, -1, -1)], dt=2.0, nsteps=20, neigh=(1, 7.22),
                     integ=("beeman", ""))
+    if name == "lj_fastlj":
+        s_ = I.lj_system(5, 0.8, 1.2, seed=25)
+        return dict(pos=s_["pos"], L=s_["L"], symbol="Ar", Z=18, vel=s_["vel"], cm="linkedcell",
+                    cm_args="cutoff 8.5 nx 3 ny 3 nz 3", pots=[("fastlj", LJ_AR + " bins 500", -1, -1)], dt=2.0,
+                    nsteps=30, neigh=(1, 8.5))
     if name == "lj_auto":
         pos, L = I.fcc_crystal3d(10, 10, 10, 5.26)
         m = np.full(len(pos), I.MASSES["Ar"])
@@ -128,7 +133,9 @@ def workload(name: str) -> dict:
     raise KeyError(name)
 
 
-GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_auto", "lj_nx2"]
+GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_fastlj", "lj_auto",
+                "lj_nx2"]
+FP64_ONLY_CASES = {"lj_fastlj"}  # fastlj has no mixed-precision form
 # integrators other than velocityverlet (fixtures from the reference's own plugins)
 INTEG_CASES = ["lj_integ_euler", "lj_integ_leapfrog", "lj_integ_verlet", "lj_integ_beeman", "lj_integ_nosehoover",
                "sc_integ_beeman"]

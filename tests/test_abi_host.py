@@ -138,3 +138,18 @@ def test_gupta_closed_form():
     assert mb[1] == pytest.approx(want, rel=1e-14) and mb[0] == 0.0
     with pytest.raises(SyntaxError, match="Unexpected end of input"):
         gbmd.Plugin("gupta", "A 1 r0 2 p 3 B 4 q")  # a keyword without a value
+
+
+@pytest.mark.parametrize("r", [3.3, 3.81, 6.0, 8.49])
+def test_fastlj_functionals_are_the_table_steps(r):
+    # plugins/fastlj.cc:38-73: LJ at the lower edge of bin floor(bins r / cutoff)
+    sigma, eps, rc, bins = 3.405, 0.0103, 8.5, 500
+    p = gbmd.Plugin("fastlj", f"sigma {sigma} epsilon {eps} cutoff {rc}")
+    assert p["bins"] == "500" and p.cutoff() == rc
+    rk = rc * math.floor(bins * r / rc) / bins
+    r6 = (sigma / rk) ** 6
+    assert p.pair_energy(r) == pytest.approx(4 * eps * (r6 * r6 - r6), rel=1e-14)
+    f = p.pair_force([0.0, 0.0, r])
+    assert f[2] == pytest.approx(r * -48 * (eps / rk ** 2) * (r6 * r6 - 0.5 * r6), rel=1e-14)
+    lj = gbmd.Plugin("lennardjones", f"sigma {sigma} epsilon {eps} cutoff {rc}")
+    assert p.pair_energy(r) == pytest.approx(lj.pair_energy(rk), rel=1e-13)

@@ -111,7 +111,7 @@ typedef struct gbmd_plugin gbmd_plugin;
 /* Creates a plugin from its LPMD name and argument string, as
  * PluginManager::LoadPlugin(name, id, args) + extern "C" create(std::string args) do
  * (liblpmd/plugins/pluginmanager.cc:123-143, liblpmd/lpmd/plugin.h:45-46).  Names:
- * "linkedcell", "verletlist", "minimumimage", "lennardjones", "fastlj", "suttonchen", "gupta",
+ * "linkedcell", "verletlist", "minimumimage", "lcbinary", "lennardjones", "fastlj", "suttonchen", "gupta",
  * "finnissinclair", "finnissinclair-ext", "velocityverlet", "euler", "leapfrog", "verlet",
  * "beeman", "nosehoover".  Arguments are parsed as
  * Module::ProcessArguments does (liblpmd/plugins/module.cc:77-103): whitespace-separated

@@ -10,7 +10,7 @@ simulation it describes through libgbmd:
   input crystal3d type=fcc|bcc|sc|hcp symbol=X nx= ny= nz=     initial lattice (crystal3d)
   input module=lpmd|xyz file=F                                 first configuration of a file
   prepare temperature t=T [seed=S]                             velocities (see below)
-  use linkedcell|verletlist|minimumimage|lennardjones|suttonchen|gupta|finnissinclair|
+  use linkedcell|verletlist|minimumimage|lcbinary|lennardjones|fastlj|suttonchen|gupta|finnissinclair|
       finnissinclair-ext|velocityverlet|euler|leapfrog|verlet|
       beeman|nosehoover [as id] ... enduse                     the timestep's plugins
   cellmanager <id> / potential <id> A B / integrator <id>      wiring (ids of use blocks)
@@ -47,7 +47,7 @@ import numpy as np
 from . import formats as F
 from . import inputs as I
 
-TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lennardjones", "fastlj", "suttonchen", "gupta",
+TIMESTEP_PLUGINS = {"linkedcell", "verletlist", "minimumimage", "lcbinary", "lennardjones", "fastlj", "suttonchen", "gupta",
                     "finnissinclair",
                     "finnissinclair-ext", "velocityverlet", "euler", "leapfrog", "verlet", "beeman", "nosehoover"}
 MODIFIER_PLUGINS = {"tempscaling", "temperature", "berendsen"}

@@ -179,6 +179,21 @@ PluginSpec make_plugin(const std::string& name, const std::string& args) {
       std::string r = p.get("rebuild");
       p.cm.rebuild = (r == "each") ? REBUILD_EACH : (r == "skin") ? REBUILD_SKIN : REBUILD_BOTH;
     }
+  } else if (name == "lcbinary") {
+    // plugins/lcbinary.cc:9-31: cutoff 7.0, nx ny nz 0, mode noauto; any zero count means auto
+    p.kind = GBMD_KIND_CELLMANAGER;
+    defaulted("cutoff", "7.0");
+    defaulted("nx", "0");
+    defaulted("ny", "0");
+    defaulted("nz", "0");
+    defaulted("mode", "noauto");
+    p.cm.kind = CM_LCBINARY;
+    p.cm.cutoff = num(p, "cutoff");
+    p.cm.nx = std::atoi(p.get("nx").c_str());
+    p.cm.ny = std::atoi(p.get("ny").c_str());
+    p.cm.nz = std::atoi(p.get("nz").c_str());
+    p.cm.mode_auto = p.cm.nx == 0 || p.cm.ny == 0 || p.cm.nz == 0 || p.get("mode") == "auto" || p.get("mode") == "AUTO";
+    if (has("skin")) p.cm.skin = num(p, "skin");
   } else if (name == "minimumimage") {
     p.kind = GBMD_KIND_CELLMANAGER;
     defaulted("cutoff", "0.0");

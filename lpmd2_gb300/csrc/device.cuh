@@ -89,7 +89,7 @@ struct SysState {
   int force_rebuild;
   int max_count;
   int error;
-  int pad0;
+  int collide;             // lcbinary: a sub-cell of the last re-sort holds two atoms
   long long rebuilds;
   long long ucalls;        // emulated UpdateCell calls (verletlist "each")
   long long step;

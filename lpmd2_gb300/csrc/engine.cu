@@ -45,6 +45,25 @@ void ck(cudaError_t e, const char* what) {
 #define CK(x) ck((x), #x)
 
 // Automatic subdivision of LinkedCell, plugins/linkedcell.cc:146-204 (one axis).
+// LCBinary's automatic grid (plugins/lcbinary.cc:52-107): sub-cells near cutoff/5 wide, the
+// count rounded up to even.
+int lcb_auto_n(double len, double cutoff) {
+  double fnn = cutoff / 5.0;
+  int n = 1;
+  for (;;) {
+    double previo = std::fabs(len / n - fnn);
+    n++;
+    double actual = std::fabs(len / n - fnn);
+    if (actual < 1E-3) break;
+    if (actual > previo) {
+      n--;
+      break;
+    }
+  }
+  if ((n % 2) != 0) n++;
+  return n;
+}
+
 int lc_auto_n(double len, double cutoff) {
   double fnn = (cutoff / 2.5);
   int n = 1;
@@ -268,6 +287,63 @@ struct Engine::Impl {
   int ntiles = 0;
   int total_cells = 0;
   bool any_list = false;
+  std::vector<std::array<int, 3>> lcb_n;  // lcbinary grids per system (they only grow)
+
+  // LCBinary's stencil half-width: ceil(cutoff / d - 0.5) with d the narrowest sub-cell edge
+  // (plugins/lcbinary.cc:113-119).
+  static int lcb_side(const double* L, const int* n, double cutoff) {
+    double d = L[0] / double(n[0]);
+    if (L[1] / double(n[1]) < d) d = L[1] / double(n[1]);
+    if (L[2] / double(n[2]) < d) d = L[2] / double(n[2]);
+    int side = int(std::ceil((cutoff / d) - 0.5));
+    return side < 0 ? 0 : side;
+  }
+  bool lcb_exact() const { return cm.kind == CM_LCBINARY && precision == PREC_FP64; }
+
+  // After a re-sort on lcbinary grids: while some sub-cell holds two atoms, grow that system's
+  // grid by 2 per axis and re-sort (LCBinary::UpdateCell, plugins/lcbinary.cc:176-193).
+  void lcb_grow_until_single(cudaStream_t s) {
+    for (int round = 0; round < 64; ++round) {
+      k_binary_collide<<<nblocks(D.total_cells, 256), 256, 0, s>>>(D);
+      launched();
+      std::vector<SysState> hs(nsys);
+      CK(cudaMemcpyAsync(hs.data(), d_sst, sizeof(SysState) * nsys, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      bool any = false;
+      for (int q = 0; q < nsys; ++q)
+        if (hs[q].collide) {
+          any = true;
+          for (int a = 0; a < 3; ++a) lcb_n[q][a] += 2;
+        }
+      if (!any) return;
+      k_binary_clear<<<1, 256, 0, s>>>(D);
+      launched();
+      // new geometry for every system (cell bases move), then the same re-sort again
+      total_cells = 0;
+      for (int q = 0; q < nsys; ++q) {
+        SysDev& S = sysd[q];
+        for (int a = 0; a < 3; ++a) S.n[a] = lcb_n[q][a];
+        S.lc_side = lcb_side(S.L, S.n, cm.cutoff);
+        for (int a = 0; a < 3; ++a) {
+          S.d[a] = S.L[a] / (double)S.n[a];
+          S.df[a] = (float)S.d[a];
+          S.ninv[a] = (double)S.n[a] / S.L[a];
+        }
+        S.ncells = S.n[0] * S.n[1] * S.n[2];
+        S.cell_base = total_cells;
+        total_cells += S.ncells;
+      }
+      for (int a = 0; a < 3; ++a) st.cell_grid[a] = sysd[0].n[a];
+      free_cells();
+      alloc_cells(total_cells);
+      alloc_list(0);
+      upload_sysd();
+      k_cell_centres<<<nblocks(total_cells, 256), 256, 0, s>>>(D);
+      launched();
+      launch_rebuild_kernels(s);
+    }
+    throw Error(7, "lcbinary: no collision-free grid after 64 enlargements");
+  }
 
   Dev D{};
   SysDev* d_sysd = nullptr;
@@ -625,6 +701,24 @@ struct Engine::Impl {
         } else {
           mode = NB_LIST;
         }
+      } else if (cm.kind == CM_LCBINARY) {
+        // FP64: the reference's sub-cell stencil exactly (NB_CELLS on the lcbinary grid, which
+        // grows when two atoms share a sub-cell); mixed: the complete Verlet list
+        if ((int)lcb_n.size() != nsys) lcb_n.assign(nsys, {0, 0, 0});
+        int* n = lcb_n[s].data();
+        if (n[0] == 0)
+          for (int q = 0; q < 3; ++q)
+            n[q] = cm.mode_auto ? lcb_auto_n(L[q], cm.cutoff) : (q == 0 ? cm.nx : q == 1 ? cm.ny : cm.nz);
+        if (n[0] <= 0 || n[1] <= 0 || n[2] <= 0) throw Error(1, "lcbinary: nx, ny and nz must be positive");
+        double skin = opt_skin >= 0 ? opt_skin : (cm.skin >= 0 ? cm.skin : 0.1 * rc);
+        rl = rc + skin;
+        if (precision == PREC_FP64) {
+          mode = NB_CELLS;
+          for (int q = 0; q < 3; ++q) S.n[q] = n[q];
+          S.lc_side = lcb_side(L, n, cm.cutoff);
+        } else {
+          mode = rl < 0.5 * std::min(L[0], std::min(L[1], L[2])) ? NB_LIST : NB_ALLPAIRS;
+        }
       } else {  // verletlist
         if (std::fabs(cm.cutoff) < 1E-10) throw Error(3, "verletlist: No cutoff was defined");
         if (cm.skin >= 0 || opt_skin >= 0) {
@@ -749,6 +843,11 @@ struct Engine::Impl {
 
   void launch_rebuild(cudaStream_t s) {
     Range r("gbmd:enqueue_rebuild");
+    launch_rebuild_kernels(s);
+    if (lcb_exact() && !capturing) lcb_grow_until_single(s);
+  }
+
+  void launch_rebuild_kernels(cudaStream_t s) {
     const unsigned nb = nblocks(N, 256);
     mark_begin(s, T_REBUILD);
     k_bin<<<nb, 256, 0, s>>>(D);
@@ -1213,7 +1312,7 @@ struct Engine::Impl {
       check_launch("step");
       done = 1;
     }
-    const int gb = graph_block;
+    const int gb = lcb_exact() ? 0 : graph_block;  // lcbinary grows its grid on the host
     if (graph_mode > 0 && gb > 0) {
       // a block of gb steps flips the buffers gb times: keep its parity even so one graph
       // serves every block
@@ -1379,6 +1478,7 @@ void Engine::get_atoms(int sys, double* pos, double* vel, double* acc) {
 
 void Engine::set_cell_manager(const CellManagerCfg& cfg) {
   d_->cm = cfg;
+  d_->lcb_n.clear();
   d_->have_cm = true;
   d_->pending_ucalls = 1;  // Configuration::SetCellManager calls UpdateCell once
   d_->configured = false;
@@ -1534,7 +1634,7 @@ void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t*
       throw Error(1, "rcut exceeds the neighbour-list radius (cutoff + skin)");
   }
   int half = 0;
-  if (!full) half = (I.cm.kind == CM_LINKEDCELL) ? 1 : 2;
+  if (!full) half = (I.cm.kind == CM_LINKEDCELL || I.cm.kind == CM_LCBINARY) ? 1 : 2;
   const double rc2 = rcut * rcut;
   const float lo = (float)(rc2 * (1.0 - 8e-6)), hi = (float)(rc2 * (1.0 + 8e-6));
   const bool mixed = I.precision == PREC_MIXED;

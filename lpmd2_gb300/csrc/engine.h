@@ -6,7 +6,7 @@
 //   Engine::do_steps        SimulationEngine::DoStep + TwoStepIntegrator::Advance
 //                           liblpmd/simulation/simulationbuilder.cc:126-136,
 //                           liblpmd/simulation/twostepintegrator.cc:12-68
-//   CellManagerCfg          LinkedCell / VerletListCellManager / MinimumImage plugins
+//   CellManagerCfg          LinkedCell / VerletListCellManager / MinimumImage / LCBinary plugins
 //   PotParams               LennardJones / FastLJ / SuttonChen / FinnisSinclair(-Ext) / Gupta plugins
 #pragma once
 
@@ -25,7 +25,7 @@ struct Error : std::runtime_error {
 };
 
 enum PotKind { POT_LJ = 1, POT_SC = 2, POT_FS = 3, POT_FSEXT = 4, POT_GUPTA = 5, POT_FASTLJ = 6 };
-enum CmKind { CM_LINKEDCELL = 1, CM_VERLETLIST = 2, CM_MINIMUMIMAGE = 3 };
+enum CmKind { CM_LINKEDCELL = 1, CM_VERLETLIST = 2, CM_MINIMUMIMAGE = 3, CM_LCBINARY = 4 };
 enum NbMode { NB_ALLPAIRS = 0, NB_CELLS = 1, NB_LIST = 2 };
 enum Rebuild { REBUILD_SKIN = 0, REBUILD_EACH = 1, REBUILD_BOTH = 2 };
 enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };

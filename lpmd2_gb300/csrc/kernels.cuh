@@ -165,6 +165,20 @@ __global__ void k_scan(Dev D) {
   }
 }
 
+// LCBinary::UpdateCell keeps at most one atom per sub-cell (plugins/lcbinary.cc:162-193): flags
+// the systems whose re-sort put two atoms into one cell (their grid then grows by 2 per axis).
+__global__ void k_binary_collide(Dev D) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= D.total_cells) return;
+  const int s = D.cell_sys[g];
+  if (!D.sysd[s].active || !D.sst[s].need_rebuild) return;
+  if (D.ccnt[g] > 1) atomicOr(&D.sst[s].collide, 1);
+}
+
+__global__ void k_binary_clear(Dev D) {
+  for (int s = threadIdx.x; s < D.nsys; s += blockDim.x) D.sst[s].collide = 0;
+}
+
 __global__ void k_scatter(Dev D) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N) return;

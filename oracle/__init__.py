@@ -73,6 +73,8 @@ def _port():
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.orc_sim_set_verletlist.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int64, ctypes.c_int64]
     lib.orc_sim_set_minimumimage.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    lib.orc_sim_set_lcbinary.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int]
     lib.orc_sim_add_potential.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int]
     lib.orc_sim_set_velocityverlet.argtypes = [ctypes.c_void_p, ctypes.c_double]
@@ -152,6 +154,10 @@ class PortSim:
                                                    int(kw.get("maxneighbors", 80)), int(kw.get("each", 5))))
         elif name == "minimumimage":
             _check(self.lib.orc_sim_set_minimumimage(self.h, float(kw.get("cutoff", 0.0))))
+        elif name == "lcbinary":
+            auto = kw.get("mode", "noauto") in ("auto", "AUTO")
+            _check(self.lib.orc_sim_set_lcbinary(self.h, float(kw.get("cutoff", 7.0)), int(kw.get("nx", 0)),
+                                                 int(kw.get("ny", 0)), int(kw.get("nz", 0)), int(auto)))
         else:
             raise OracleError(f"unknown cell manager {name}")
 

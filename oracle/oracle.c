@@ -53,6 +53,8 @@ typedef struct {
   int64_t maxneighbors, each, step_count, old_size;
   int64_t* nv;
   int64_t* vlist; /* n * maxneighbors */
+  /* lcbinary: the atom of every sub-cell (-1: none) */
+  int64_t* binlist;
 } orc_cm;
 
 struct orc_sim {
@@ -187,6 +189,7 @@ static void cm_free(orc_cm* cm) {
   free(cm->cached_rcut_full);
   free(cm->nv);
   free(cm->vlist);
+  free(cm->binlist);
   free(cm);
 }
 
@@ -413,6 +416,147 @@ static int vl_list(orc_sim* s, orc_cm* cm, int64_t i, int full, double rcu, int6
   return ORC_OK;
 }
 
+/* LCBinary automatic grid, plugins/lcbinary.cc:52-107: sub-cells near cutoff/5, count made even. */
+static int lcb_auto_n(double len, double cutoff) {
+  double fnn = cutoff / 5.0;
+  int n = 1;
+  while (1) {
+    double previo = fabs(len / n - fnn);
+    n++;
+    double actual = fabs(len / n - fnn);
+    if (actual < 1E-3)
+      break;
+    else if (actual > previo) {
+      n--;
+      break;
+    }
+  }
+  if ((n % 2) != 0)
+    n++;
+  return n;
+}
+
+/* The sub-cell of a position (cell.Fractional, floor, wrap above only), plugins/lcbinary.cc:163-178. */
+static int64_t lcb_cell(const orc_cm* cm, const double L[3], const double* x) {
+  int i = (int)floor(cm->nx * (x[0] / L[0]));
+  int j = (int)floor(cm->ny * (x[1] / L[1]));
+  int k = (int)floor(cm->nz * (x[2] / L[2]));
+  if (i > cm->nx - 1)
+    i -= cm->nx;
+  if (j > cm->ny - 1)
+    j -= cm->ny;
+  if (k > cm->nz - 1)
+    k -= cm->nz;
+  return (int64_t)k * (cm->nx * cm->ny) + (int64_t)j * cm->nx + i;
+}
+
+/* LCBinary::UpdateCell, plugins/lcbinary.cc:50-193: grid (automatic once), sub-cell stencil of
+ * half-width ceil(cutoff/d - 0.5) with one wrap per axis, one atom per sub-cell (the last one
+ * binned); a shared sub-cell grows every count by 2 and starts over. */
+static int lcb_update_cell(orc_sim* s, orc_cm* cm) {
+  for (int round = 0; round < 1000; ++round) {
+    if (cm->mode_auto) {
+      cm->nx = lcb_auto_n(s->L[0], cm->cutoff);
+      cm->ny = lcb_auto_n(s->L[1], cm->cutoff);
+      cm->nz = lcb_auto_n(s->L[2], cm->cutoff);
+      cm->mode_auto = 0;
+    }
+    const int nx = cm->nx, ny = cm->ny, nz = cm->nz;
+    if (nx <= 0 || ny <= 0 || nz <= 0)
+      return ORC_ERR_INVALID;
+    const int64_t ncell = (int64_t)nx * ny * nz;
+    if (cm->subcell == NULL) {
+      double d = s->L[0] / (double)nx;
+      if (s->L[1] / (double)ny < d)
+        d = s->L[1] / (double)ny;
+      if (s->L[2] / (double)nz < d)
+        d = s->L[2] / (double)nz;
+      int side = (int)ceil((cm->cutoff / d) - 0.5);
+      cm->side = side;
+      cm->cells_inside = (2 * side + 1) * (2 * side + 1) * (2 * side + 1);
+      cm->subcell = (int*)malloc(sizeof(int) * (size_t)(ncell * cm->cells_inside));
+      if (!cm->subcell)
+        return ORC_ERR_NOMEM;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) {
+            int r = 0;
+            int64_t q = (int64_t)k * (nx * ny) + j * nx + i;
+            for (int dz = -side; dz <= side; ++dz)
+              for (int dy = -side; dy <= side; ++dy)
+                for (int dx = -side; dx <= side; ++dx) {
+                  int z0 = i + dx, z1 = j + dy, z2 = k + dz;
+                  if (z0 < 0)
+                    z0 += nx;
+                  else if (z0 > nx - 1)
+                    z0 -= nx;
+                  if (z1 < 0)
+                    z1 += ny;
+                  else if (z1 > ny - 1)
+                    z1 -= ny;
+                  if (z2 < 0)
+                    z2 += nz;
+                  else if (z2 > nz - 1)
+                    z2 -= nz;
+                  if (z0 < 0 || z0 >= nx || z1 < 0 || z1 >= ny || z2 < 0 || z2 >= nz)
+                    return ORC_ERR_INVALID; /* a stencil wider than the grid: out of the reference's range */
+                  cm->subcell[q * cm->cells_inside + (r++)] = z2 * (nx * ny) + z1 * nx + z0;
+                }
+          }
+    }
+    if (cm->binlist == NULL) {
+      cm->binlist = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncell);
+      if (!cm->binlist)
+        return ORC_ERR_NOMEM;
+    }
+    for (int64_t c = 0; c < ncell; ++c)
+      cm->binlist[c] = -1;
+    int update = 0;
+    for (int64_t r = 0; r < s->n; ++r) {
+      int64_t q = lcb_cell(cm, s->L, &s->pos[3 * r]);
+      if (q < 0 || q >= ncell)
+        return ORC_ERR_INVALID;
+      if (cm->binlist[q] != -1)
+        update = 1;
+      cm->binlist[q] = r;
+    }
+    if (!update)
+      return ORC_OK;
+    cm->nx += 2;
+    cm->ny += 2;
+    cm->nz += 2;
+    free(cm->subcell);
+    cm->subcell = NULL;
+    free(cm->binlist);
+    cm->binlist = NULL;
+  }
+  return ORC_ERR_INVALID;
+}
+
+/* LCBinary::BuildNeighborList, plugins/lcbinary.cc:216-254: the stencil's atoms, lower indices
+ * only for a half list. */
+static int lcb_list(orc_sim* s, orc_cm* cm, int64_t i, int full, double rcut, int64_t* cnt) {
+  *cnt = 0;
+  const double* xi = &s->pos[3 * i];
+  const int* c = &cm->subcell[lcb_cell(cm, s->L, xi) * cm->cells_inside];
+  for (int q = 0; q < cm->cells_inside; ++q) {
+    int64_t z = cm->binlist[c[q]];
+    if ((z < 0) || (z == i))
+      continue;
+    if ((z > i) && (full == 0))
+      continue;
+    double rij[3];
+    orc_displacement(s->L, xi, &s->pos[3 * z], rij);
+    double r2 = sqmod(rij);
+    if (r2 < rcut * rcut) {
+      int e = push_pair(s, cnt, z, rij, r2);
+      if (e)
+        return e;
+    }
+  }
+  return ORC_OK;
+}
+
 /* MinimumImageCellManager, plugins/minimumimage.cc:55-100. */
 static int mi_update_cell(orc_sim* s, orc_cm* cm) {
   if (fabs(cm->cutoff) < 1E-10) {
@@ -455,6 +599,8 @@ static int cm_update_cell(orc_sim* s) {
     return vl_update_cell(s, cm);
   case ORC_CM_MINIMUMIMAGE:
     return mi_update_cell(s, cm);
+  case ORC_CM_LCBINARY:
+    return lcb_update_cell(s, cm);
   }
   return ORC_ERR_INVALID;
 }
@@ -468,6 +614,8 @@ static int cm_list(orc_sim* s, int64_t i, int full, double rcut, int64_t* cnt) {
     return vl_list(s, cm, i, full, rcut, cnt);
   case ORC_CM_MINIMUMIMAGE:
     return mi_list(s, i, full, rcut, cnt);
+  case ORC_CM_LCBINARY:
+    return lcb_list(s, cm, i, full, rcut, cnt);
   }
   return ORC_ERR_INVALID;
 }
@@ -924,6 +1072,20 @@ int orc_sim_set_verletlist(orc_sim* s, double cutoff, int64_t maxneighbors, int6
   cm->extcut = 1.08 * cutoff;
   cm->step_count = 0;
   cm->old_size = 0;
+  return set_cm(s, cm);
+}
+
+int orc_sim_set_lcbinary(orc_sim* s, double cutoff, int nx, int ny, int nz, int mode_auto) {
+  orc_cm* cm = (orc_cm*)calloc(1, sizeof(orc_cm));
+  if (!cm)
+    return ORC_ERR_NOMEM;
+  cm->kind = ORC_CM_LCBINARY;
+  cm->cutoff = cutoff;
+  cm->nx = nx;
+  cm->ny = ny;
+  cm->nz = nz;
+  /* plugins/lcbinary.cc:23-28: a zero count or mode auto selects the automatic grid */
+  cm->mode_auto = mode_auto || nx == 0 || ny == 0 || nz == 0;
   return set_cm(s, cm);
 }
 

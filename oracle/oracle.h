@@ -19,6 +19,7 @@
  *                                                    plugins/finnissinclair-ext.cc:85-128
  *   - Gupta functionals                              plugins/gupta.cc:52-75
  *   - FastLJ tables and lookups                      plugins/fastlj.cc:38-73
+ *   - LCBinary grid, growth and neighbour lists      plugins/lcbinary.cc:50-254
  *   - CombinedPotential::UpdateForces                liblpmd/lpmd/combinedpotential.h:39-52
  *   - TwoStepIntegrator::Advance + VelocityVerlet    liblpmd/simulation/twostepintegrator.cc:12-68,
  *                                                    plugins/velocityverlet.cc:55-75,
@@ -53,7 +54,7 @@ enum {
   ORC_ERR_CAPACITY = 5      /* caller buffer too small */
 };
 
-enum { ORC_CM_LINKEDCELL = 1, ORC_CM_VERLETLIST = 2, ORC_CM_MINIMUMIMAGE = 3 };
+enum { ORC_CM_LINKEDCELL = 1, ORC_CM_VERLETLIST = 2, ORC_CM_MINIMUMIMAGE = 3, ORC_CM_LCBINARY = 4 };
 
 enum { ORC_POT_LJ = 1, ORC_POT_SC = 2, ORC_POT_FS = 3, ORC_POT_FSEXT = 4, ORC_POT_GUPTA = 5, ORC_POT_FASTLJ = 6 };
 
@@ -99,6 +100,7 @@ int orc_sim_get_atoms(const orc_sim* s, double* pos, double* vel, double* acc);
 int orc_sim_set_linkedcell(orc_sim* s, double cutoff, int nx, int ny, int nz, int mode_auto);
 int orc_sim_set_verletlist(orc_sim* s, double cutoff, int64_t maxneighbors, int64_t each);
 int orc_sim_set_minimumimage(orc_sim* s, double cutoff);
+int orc_sim_set_lcbinary(orc_sim* s, double cutoff, int nx, int ny, int nz, int mode_auto);
 
 /* Appends a potential to the CombinedPotential with SetValidSpecies(s1, s2).
  * params: LJ {sigma, epsilon, cutoff}; SC {e, a, n, m, c, cutoff};

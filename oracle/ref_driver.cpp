@@ -24,6 +24,7 @@
 #include "fastlj.h"
 #include "finnissinclair.h"
 #include "gupta.h"
+#include "lcbinary.h"
 #include "lennardjones.h"
 #include "linkedcell.h"
 #include "minimumimage.h"
@@ -68,6 +69,7 @@ CellManager* make_cm(const std::string& name, const std::string& args) {
   if (name == "linkedcell") return new LinkedCell(args);
   if (name == "verletlist") return new VerletListCellManager(args);
   if (name == "minimumimage") return new MinimumImageCellManager(args);
+  if (name == "lcbinary") return new LCBinary(args);
   return nullptr;
 }
 

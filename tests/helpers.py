@@ -113,6 +113,13 @@ def workload(name: str) -> dict:
                     cm="linkedcell", cm_args="cutoff 7.22 nx 3 ny 3 nz 3",
                     pots=[("suttonchen", SC_CU, -1, -1)], dt=2.0, nsteps=20, neigh=(1, 7.22),
                     integ=("beeman", ""))
+    if name.startswith("lj_lcbinary"):
+        # automatic grid (sub-cells of about cutoff/5: the stencil stops short of the cutoff), or
+        # a coarse 4x4x4 grid that has to grow until no sub-cell holds two atoms
+        s_ = I.lj_system(5, 0.8, 1.2, seed=27)
+        args = "cutoff 8.5 mode auto" if name == "lj_lcbinary" else "cutoff 8.5 nx 4 ny 4 nz 4"
+        return dict(pos=s_["pos"], L=s_["L"], symbol="Ar", Z=18, vel=s_["vel"], cm="lcbinary", cm_args=args,
+                    pots=[("lennardjones", LJ_AR, -1, -1)], dt=2.0, nsteps=30, neigh=(1, 8.5))
     if name == "lj_fastlj":
         s_ = I.lj_system(5, 0.8, 1.2, seed=25)
         return dict(pos=s_["pos"], L=s_["L"], symbol="Ar", Z=18, vel=s_["vel"], cm="linkedcell",
@@ -134,7 +141,7 @@ def workload(name: str) -> dict:
 
 
 GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_fastlj", "lj_auto",
-                "lj_nx2"]
+                "lj_nx2", "lj_lcbinary", "lj_lcbinary_grow"]
 FP64_ONLY_CASES = {"lj_fastlj"}  # fastlj has no mixed-precision form
 # integrators other than velocityverlet (fixtures from the reference's own plugins)
 INTEG_CASES = ["lj_integ_euler", "lj_integ_leapfrog", "lj_integ_verlet", "lj_integ_beeman", "lj_integ_nosehoover",

@@ -512,6 +512,7 @@ def make_batch(systems, precision: str, device: int, params: dict):
     b.set_precision(precision)
     b.set_option("graph_block", GRAPH_BLOCK)
     b.set_option("cell_scale", params["cell_scale"])
+    b.set_option("lanes_per_atom", params.get("lanes_per_atom", 1))
     return b
 
 

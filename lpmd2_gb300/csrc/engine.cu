@@ -279,6 +279,7 @@ struct Engine::Impl {
   double opt_skin = -1.0;
   int graph_block = 10;
   int graph_mode = 2;  // 0 direct, 1 captured, 2 captured with conditional rebuild
+  int lanes = 1;       // lanes per atom of the mixed LJ force pass
   int stencil_r = 1;
   int log_cap = 1024;
 
@@ -907,7 +908,15 @@ struct Engine::Impl {
       }
       if (mixed) {
         const bool species = P.spc_sum >= 0;
-        if (pair_kind(P.kind)) {
+        if (pair_kind(P.kind) && lanes > 1) {
+          const unsigned g = (unsigned)ntiles * lanes;
+          if (lanes == 2)
+            species ? k_force32_lanes<1, 2><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 2><<<g, TILE, 0, s>>>(D, P, sp);
+          else if (lanes == 4)
+            species ? k_force32_lanes<1, 4><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 4><<<g, TILE, 0, s>>>(D, P, sp);
+          else
+            species ? k_force32_lanes<1, 8><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 8><<<g, TILE, 0, s>>>(D, P, sp);
+        } else if (pair_kind(P.kind)) {
           if (species)
             k_force32<PC_PAIR, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
           else
@@ -1547,6 +1556,13 @@ void Engine::set_option(const std::string& key, const std::string& value) {
   }
   if (key == "stream_priority") {  // 1: highest, 0: lowest (default); replaces the stream
     I.set_priority(v != 0.0 ? 1 : 0);
+    return;
+  }
+  if (key == "lanes_per_atom") {  // mixed LJ force pass: 1 (bulk-copy ring), 2, 4 or 8 lanes per atom
+    const int l = (int)v;
+    if (l != 1 && l != 2 && l != 4 && l != 8) throw Error(1, "lanes_per_atom must be 1, 2, 4 or 8");
+    I.lanes = l;
+    I.drop_graph();
     return;
   }
   if (key == "skin") {

@@ -517,6 +517,191 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
 }
 
 // ------------------------------------------------------------------------------------------
+// Mixed LJ force pass with LANES lanes per atom (LANES = 2, 4, 8: 16, 8 or 4 atoms per warp),
+// for systems too small to fill the GPU one lane per atom.  The atom's list groups go
+// round-robin to its lanes (plain cached loads instead of the bulk-copy ring); each group is
+// evaluated and summed exactly as in k_force32, and the lanes' fixed-point partials are
+// combined with integer shuffles, so the forces are bitwise those of k_force32.  Energy and
+// stress partials are rounded to fixed point per lane (a 2^-32 eV-scale difference).  A tile
+// of 128 atoms is spread over LANES blocks of 128 threads.
+// ------------------------------------------------------------------------------------------
+
+template <int SPECIES, int LANES>
+__global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(Dev D, PotParams P, StepParams sp) {
+  __shared__ float4 shifts[125];
+  constexpr int APB = TILE / LANES;  // atoms per block
+  const int tile = blockIdx.x / LANES, part = blockIdx.x % LANES;
+  const int s = D.tile_sys[tile];
+  const SysDev& S = D.sysd[s];
+  if (!S.active) {  // whole block: one tile belongs to one system
+    if (part == 0 && sp.epi == EPI_KICK_DRIFT && sp.last) hold_tile(D, S, tile, true);
+    return;
+  }
+  load_shifts(S, shifts);
+  const int sub = threadIdx.x % LANES;
+  const int slot = part * APB + (int)threadIdx.x / LANES;  // atom within the tile
+  const int li = D.tile_first[tile] - (int)S.atom_base + slot;
+  const long long i = S.atom_base + li;
+  const bool active = slot < D.tile_count[tile];
+  const float4* __restrict__ g32 = D.g32 + S.atom_base;
+  Fix fqx, fqy, fqz;
+  float ep = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  const float rc2_lo = P.f[12], rc2_hi = P.f[13];
+  unsigned rechecks = 0;
+  bool bad = false;
+  const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int ti = __float_as_int(gi.w);
+  const int na = S.natoms;
+  const int cnt = active ? D.ncount[i] : 0;
+  const int ng = (cnt + 3) >> 2;
+  constexpr unsigned NO_BAND = 0xffffffffu;
+  unsigned band_e = NO_BAND;
+  bool band_more = false;
+  auto pair = [&](unsigned e, bool valid, float& dx, float& dy, float& dz) -> float {
+    const int j = (int)(e & LOCAL_MASK);
+    const float4 gj = g32[j];
+    const float4 sh = shifts[e >> CODE_SHIFT];
+    dx = (sh.x + gj.x) - gi.x;
+    dy = (sh.y + gj.y) - gi.y;
+    dz = (sh.z + gj.z) - gi.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    bool in = valid && r2 < rc2_lo;
+    if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
+      if (band_e == NO_BAND)
+        band_e = e;
+      else
+        band_more = true;
+    }
+    if (SPECIES) in = in && applies_to(P.spc_sum, ti, __float_as_int(gj.w));
+    float g, en;
+    lj_pair32(P, rcp_approx(r2), g, en);
+    g = in ? g : 0.0f;
+    ep += in ? en : 0.0f;
+    const float fx = g * dx, fy = g * dy, fz = g * dz;
+    sxx = fmaf(fx, dx, sxx);
+    sxy = fmaf(fx, dy, sxy);
+    sxz = fmaf(fx, dz, sxz);
+    syy = fmaf(fy, dy, syy);
+    syz = fmaf(fy, dz, syz);
+    szz = fmaf(fz, dz, szz);
+    return g;
+  };
+  const uint4* L = active ? list_group(D, S, li, 0) : nullptr;
+  for (int q = sub; q < ng; q += LANES) {
+    const uint4 cur = __ldg(L + (long long)q * na);
+    const int rem = cnt - 4 * q;
+    float ax, ay, az, bx, by, bz;
+    float g0 = pair(cur.x, true, ax, ay, az);
+    float g1 = pair(cur.y, rem > 1, bx, by, bz);
+    float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
+    g0 = pair(cur.z, rem > 2, ax, ay, az);
+    g1 = pair(cur.w, rem > 3, bx, by, bz);
+    gx = fmaf(g1, bx, fmaf(g0, ax, gx));
+    gy = fmaf(g1, by, fmaf(g0, ay, gy));
+    gz = fmaf(g1, bz, fmaf(g0, az, gz));
+    fqx.add_scaled32(gx);
+    fqy.add_scaled32(gy);
+    fqz.add_scaled32(gz);
+    bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+  }
+  if (band_e != NO_BAND) {
+    auto settle = [&](unsigned e) {
+      const int j = (int)(e & LOCAL_MASK);
+      const float4 gj = g32[j];
+      const float4 sh = shifts[e >> CODE_SHIFT];
+      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
+      ++rechecks;
+      if (!exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) return;
+      if (SPECIES && !applies_to(P.spc_sum, ti, __float_as_int(gj.w))) return;
+      float g, en;
+      lj_pair32(P, rcp_approx(r2), g, en);
+      const float fx = g * dx, fy = g * dy, fz = g * dz;
+      fqx.add_scaled32(fx);
+      fqy.add_scaled32(fy);
+      fqz.add_scaled32(fz);
+      bad |= fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) > 4000.0f;
+      ep += en;
+      sxx = fmaf(fx, dx, sxx);
+      sxy = fmaf(fx, dy, sxy);
+      sxz = fmaf(fx, dz, sxz);
+      syy = fmaf(fy, dy, syy);
+      syz = fmaf(fy, dz, syz);
+      szz = fmaf(fz, dz, szz);
+    };
+    if (!band_more) {
+      settle(band_e);
+    } else {
+      for (int q = sub; q < ng; q += LANES) {
+        const uint4 e4 = __ldg(L + (long long)q * na);
+        const int rem = cnt - 4 * q;
+        settle(e4.x);
+        if (rem > 1) settle(e4.y);
+        if (rem > 2) settle(e4.z);
+        if (rem > 3) settle(e4.w);
+      }
+    }
+  }
+  // the atom's lanes are adjacent: exact integer sums of the fixed-point partials
+#pragma unroll
+  for (int m = 1; m < LANES; m <<= 1) {
+    fqx.hi += __shfl_xor_sync(0xffffffffu, fqx.hi, m);
+    fqx.lo += __shfl_xor_sync(0xffffffffu, fqx.lo, m);
+    fqy.hi += __shfl_xor_sync(0xffffffffu, fqy.hi, m);
+    fqy.lo += __shfl_xor_sync(0xffffffffu, fqy.lo, m);
+    fqz.hi += __shfl_xor_sync(0xffffffffu, fqz.hi, m);
+    fqz.lo += __shfl_xor_sync(0xffffffffu, fqz.lo, m);
+  }
+  double ke = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+  float d2 = 0.0f;
+  if (active && sub == 0) {
+    const long long N = D.N;
+    long long qx = fqx.value(), qy = fqy.value(), qz = fqz.value();
+    if (!sp.first) {
+      qx += D.facc[i];
+      qy += D.facc[N + i];
+      qz += D.facc[2 * N + i];
+    }
+    if (sp.last) {
+      d2 = finish_atom<1>(D, S, i, (double)qx, (double)qy, (double)qz, sp, ke, px, py, pz);
+    } else {
+      D.facc[i] = qx;
+      D.facc[N + i] = qy;
+      D.facc[2 * N + i] = qz;
+    }
+  }
+  if (active) {
+    if (rechecks) atomicAdd(&D.sst[s].rechecks, (unsigned long long)rechecks);
+    if (bad) atomicOr(&D.sst[s].error, ERR_FIXED);
+  }
+  track_displacement_warp(D, s, d2);
+  const float es = (float)(0.5 * FIX_E);
+  const float ms = -es;
+  long long v[11] = {fix64(ep * es), fix64((sxx + syy + szz) * ms), fix64(sxx * ms), fix64(sxy * ms),
+                     fix64(sxz * ms), fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms),
+                     fix64(syz * ms), fix64(szz * ms)};
+  long long tot[11];
+  block_sum<long long, 11>(v, tot);
+  if (threadIdx.x == 0) {
+    unsigned long long* acc = D.sys_acc + (long long)s * SA_LEN;
+    for (int k = 0; k < 11; ++k) atomicAdd(acc + k, (unsigned long long)tot[k]);
+  }
+  if (sp.last) {
+    const double kw = warp_sum(ke);
+    long long k4[4] = {(threadIdx.x & 31) == 0 ? __double2ll_rn(kw * FIX_KE) : 0ll, __double2ll_rn(px * FIX_KE),
+                       __double2ll_rn(py * FIX_KE), __double2ll_rn(pz * FIX_KE)};
+    long long kt[4];
+    block_sum<long long, 4>(k4, kt);
+    if (threadIdx.x == 0) {
+      unsigned long long* acc = D.sys_acc + (long long)s * SA_LEN;
+      atomicAdd(acc + SA_KE, (unsigned long long)kt[0]);
+      for (int k = 0; k < 3; ++k) atomicAdd(acc + SA_P + k, (unsigned long long)kt[1 + k]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // EAM density pass + embedding (FP64 embedding in both precisions).
 // ------------------------------------------------------------------------------------------
 

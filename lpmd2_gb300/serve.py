@@ -247,6 +247,20 @@ def summarize(results: list[JobResult], wall_s: float) -> dict:
 
 
 # ---------------------------------------------------------------------- libgbmd backend
+def lanes_for(live_atoms: int) -> int:
+    """Lanes per atom of the LJ force pass for a batch with this many live atoms: below about
+    60k atoms one lane per atom leaves the GPU partly idle.  Thresholds from GB300 timings of
+    single LJ liquids at rc 2.5 sigma (ms/step with 1/2/4/8 lanes: 864 atoms 0.050/0.041/0.038/
+    0.037; 4,000: 0.055/0.046/0.042/0.042; 16,384: 0.050/0.041/0.042/0.049; 55,296:
+    0.058/0.056/0.067/0.091; 256,000: 0.145/0.165/0.206/0.322).  Forces are the same for every
+    choice, so changing it never changes a job's trajectory."""
+    if live_atoms < 10_000:
+        return 4
+    if live_atoms < 60_000:
+        return 2
+    return 1
+
+
 class GbmdBackend:
     """Runs batches through libgbmd (mixed precision, Verlet lists, 10-step graph blocks)."""
 
@@ -293,6 +307,8 @@ class GbmdBackend:
         b.set_option("graph_block", self.graph_block)
         b.live = [int(s["natoms"]) for s in systems]
         b.high = False
+        b.kind = kind
+        b.lanes = 1
         self._prioritise(b)
         b.update_forces()
         return b
@@ -304,6 +320,10 @@ class GbmdBackend:
         if not b.high and sum(b.live) <= self.small_atoms:
             b.set_option("stream_priority", 1)
             b.high = True
+        lanes = lanes_for(sum(b.live)) if b.kind == "lj" and self.precision == "mixed" else 1
+        if lanes != b.lanes:
+            b.set_option("lanes_per_atom", lanes)
+            b.lanes = lanes
 
     def device_bytes(self, b) -> int:
         return int(b.stats()["device_bytes"])

@@ -1,5 +1,5 @@
 """The autotuner's selection logic on the CPU with a stand-in batch."""
-from lpmd2_gb300.autotune import CELL_SCALES, SKINS_SIGMA, tune_batch
+from lpmd2_gb300.autotune import CELL_SCALES, LANES_PER_ATOM, SKINS_SIGMA, tune_batch
 
 
 class Stub:
@@ -13,10 +13,14 @@ class Stub:
 
 def test_picks_fastest_and_closes_every_trial():
     closed = []
-    cost = lambda p: abs(p["skin_sigma"] - 0.3) * 10 + (0.5 if p["cell_scale"] == 2 else 0.0)  # noqa: E731
+    cost = lambda p: (abs(p["skin_sigma"] - 0.3) * 10 + (0.5 if p["cell_scale"] == 2 else 0.0)  # noqa: E731
+                      + abs(p["lanes_per_atom"] - 4) * 0.01)
     best, trials = tune_batch(lambda p: Stub(p, closed), lambda b: 1.0 + cost(b.p))
-    assert best == {"skin_sigma": 0.3, "cell_scale": 1}
-    assert len(trials) == len(SKINS_SIGMA) * len(CELL_SCALES) == len(closed)
+    assert best == {"skin_sigma": 0.3, "cell_scale": 1, "lanes_per_atom": 4}
+    # the skin x cell grid at one lane, then the other lane counts at the best grid point
+    assert len(trials) == len(SKINS_SIGMA) * len(CELL_SCALES) + len(LANES_PER_ATOM) - 1 == len(closed)
+    assert [t["lanes_per_atom"] for t in trials[-3:]] == [2, 4, 8]
+    assert all(t["skin_sigma"] == 0.3 and t["cell_scale"] == 1 for t in trials[-3:])
     assert all(s.closed for s in closed)
 
 

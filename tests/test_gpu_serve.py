@@ -3,9 +3,10 @@
 A small stream of Lennard-Jones and Sutton-Chen jobs of different sizes and lengths runs
 through the job server (continuous batching: several batches in flight on their own
 streams, finished jobs retired from a running batch).  Then some of the jobs run again
-alone, each as the only system of its batch, and their final positions, velocities and
-thermo records must match the in-mix results bit for bit (mixed precision: fixed-point sums
-make every per-system result independent of what else shares the launches).
+alone, each as the only system of its batch, and their final positions and velocities must
+match the in-mix results bit for bit (mixed precision: fixed-point force sums make every
+per-system trajectory independent of what else shares the launches, and of the lane count the
+server picks for the batch's size); thermo records match to FP32 summation order.
 """
 import numpy as np
 import pytest
@@ -63,5 +64,8 @@ def test_served_results_equal_alone():
         pos, vel, th = alone(backend, jobs[j])
         np.testing.assert_array_equal(res[j].pos, pos)
         np.testing.assert_array_equal(res[j].vel, vel)
-        np.testing.assert_array_equal(res[j].thermo["raw"], th["raw"])
+        # the lane count of the LJ force pass follows the batch's live atoms (serve.lanes_for):
+        # forces, hence trajectories, are bitwise the same for every lane count; the per-atom
+        # FP32 energy and stress sums, and the per-warp kinetic sums, are grouped differently
+        np.testing.assert_allclose(res[j].thermo["raw"], th["raw"], rtol=1e-7, atol=1e-12)
         assert res[j].thermo["step"] == jobs[j]["steps"]

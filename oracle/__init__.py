@@ -19,6 +19,7 @@ THERMO_LEN = 22
 THERMO_FIELDS = ["step", "epot", "ekin", "etot", "temperature", "virial", "px", "py", "pz",
                  "volume", "virial_pressure", "kinetic_pressure", "pressure"]
 
+INTEG_KIND = {"velocityverlet": 0, "euler": 1, "leapfrog": 2, "verlet": 3, "beeman": 4, "nosehoover": 5}
 CM_KIND = {"linkedcell": 1, "verletlist": 2, "minimumimage": 3}
 POT_KIND = {"lennardjones": 1, "suttonchen": 2, "finnissinclair": 3, "finnissinclair-ext": 4, "gupta": 5,
             "fastlj": 6}
@@ -78,6 +79,8 @@ def _port():
     lib.orc_sim_add_potential.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int]
     lib.orc_sim_set_velocityverlet.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    lib.orc_sim_set_integrator.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double]
     lib.orc_sim_update_forces.argtypes = [ctypes.c_void_p]
     lib.orc_sim_do_steps.argtypes = [ctypes.c_void_p, ctypes.c_int64, _D]
     lib.orc_sim_thermo.argtypes = [ctypes.c_void_p, _D]
@@ -167,8 +170,10 @@ class PortSim:
         p = np.array([float(kw.get(k, defaults.get(k, 0.0))) for k in POT_KEYS[name]], dtype=np.float64)
         _check(self.lib.orc_sim_add_potential(self.h, POT_KIND[name], _ptr(p), len(p), s1, s2))
 
-    def set_integrator(self, dt: float):
-        _check(self.lib.orc_sim_set_velocityverlet(self.h, float(dt)))
+    def set_integrator(self, dt: float, name: str = "velocityverlet", args: str = ""):
+        kw = parse_args(args)
+        _check(self.lib.orc_sim_set_integrator(self.h, INTEG_KIND[name], float(dt), float(kw.get("fmass", 0.0)),
+                                               float(kw.get("t", 300.0))))
 
     def update_forces(self):
         _check(self.lib.orc_sim_update_forces(self.h))
@@ -245,14 +250,14 @@ def linkedcell_geometry(L, cutoff, nx, ny, nz, mode_auto=False):
     return tuple(n), side.value, ci.value
 
 
-def run_port(pos, L, Z, mass, vel, cm, cm_args, pots, dt, nsteps, neigh=None, flags=None):
+def run_port(pos, L, Z, mass, vel, cm, cm_args, pots, dt, nsteps, neigh=None, flags=None, integrator=None):
     """Same protocol as run_reference, on the C restatement."""
     sim = PortSim(pos, L, Z, mass, vel, flags)
     sim.set_cell_manager(cm, cm_args)
     for name, args, s1, s2 in pots:
         sim.add_potential(name, args, s1, s2)
     if nsteps > 0:
-        sim.set_integrator(dt)
+        sim.set_integrator(dt, *(integrator or ("velocityverlet", "")))
     sim.update_forces()
     out = {"acc0": sim.atoms()[2], "thermo0": sim.thermo()}
     if neigh is not None:

@@ -72,6 +72,11 @@ struct orc_sim {
   orc_pot pots[ORC_MAXPOT];
   int npots;
   int have_integrator;
+  int integ;       /* ORC_INT_* */
+  double fmass, t0, friction; /* nosehoover */
+  double* old_pos; /* OldConfig positions (verlet) */
+  double* old_vel; /* OldConfig velocities (leapfrog) */
+  double* aux;     /* the previous old acceleration (beeman, nosehoover) */
   double dt;
   int initialized;
   int64_t step;
@@ -981,6 +986,9 @@ void orc_sim_destroy(orc_sim* s) {
   free(s->vel);
   free(s->acc);
   free(s->old_acc);
+  free(s->old_pos);
+  free(s->old_vel);
+  free(s->aux);
   free(s->Z);
   free(s->mass);
   free(s->flags);
@@ -1137,8 +1145,17 @@ int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparam
   return ORC_OK;
 }
 
-int orc_sim_set_velocityverlet(orc_sim* s, double dt) {
+int orc_sim_set_velocityverlet(orc_sim* s, double dt) { return orc_sim_set_integrator(s, ORC_INT_VV, dt, 0.0, 300.0); }
+
+int orc_sim_set_integrator(orc_sim* s, int kind, double dt, double fmass, double t) {
+  if (kind < ORC_INT_VV || kind > ORC_INT_NOSEHOOVER)
+    return ORC_ERR_INVALID;
+  if (kind == ORC_INT_NOSEHOOVER && !(fmass > 0.0))
+    return ORC_ERR_INVALID;
+  s->integ = kind;
   s->dt = dt;
+  s->fmass = fmass;
+  s->t0 = t;
   s->have_integrator = 1;
   return ORC_OK;
 }
@@ -1227,6 +1244,206 @@ static int vv_advance(orc_sim* s) {
   return ORC_OK;
 }
 
+/* ---- the integrators other than velocityverlet ------------------------------------------ */
+
+/* Integrator::GoBack on the backed-up copy, liblpmd/simulation/integrator.cc:31-42:
+ * positions Fit(x - v dt), velocities v - a dt. */
+static int go_back(orc_sim* s) {
+  const size_t b = sizeof(double) * 3 * (size_t)(s->n > 0 ? s->n : 1);
+  if (!s->old_pos)
+    s->old_pos = (double*)malloc(b);
+  if (!s->old_vel)
+    s->old_vel = (double*)malloc(b);
+  if (!s->aux)
+    s->aux = (double*)calloc(3 * (size_t)(s->n > 0 ? s->n : 1), sizeof(double));
+  if (!s->old_pos || !s->old_vel || !s->aux)
+    return ORC_ERR_NOMEM;
+  const double dt = s->dt;
+  for (int64_t i = 0; i < s->n; ++i) {
+    double np[3];
+    for (int q = 0; q < 3; ++q) {
+      np[q] = s->pos[3 * i + q] - s->vel[3 * i + q] * dt;
+      s->old_vel[3 * i + q] = s->vel[3 * i + q] - s->acc[3 * i + q] * dt;
+    }
+    orc_fitted_inside(s->L, np, &s->old_pos[3 * i]);
+  }
+  return ORC_OK;
+}
+
+/* Potential::UpdateForces on the backed-up configuration (its own accelerations, virial and
+ * stress; the cell manager is the shared one): the accelerations land in out[3n]. */
+static int old_config_forces(orc_sim* s, double* out) {
+  const size_t b = sizeof(double) * 3 * (size_t)s->n;
+  double* save_acc = (double*)malloc(b ? b : 1);
+  if (!save_acc)
+    return ORC_ERR_NOMEM;
+  memcpy(save_acc, s->acc, b);
+  double save_virial = s->virial, save_stress[3][3], save_energy[ORC_MAXPOT];
+  memcpy(save_stress, s->stress, sizeof(save_stress));
+  memcpy(save_energy, s->energy, sizeof(save_energy));
+  double* cur = s->pos;
+  s->pos = s->old_pos;
+  int e = orc_sim_update_forces(s);
+  s->pos = cur;
+  if (e == ORC_OK)
+    memcpy(out, s->acc, b);
+  memcpy(s->acc, save_acc, b);
+  s->virial = save_virial;
+  memcpy(s->stress, save_stress, sizeof(save_stress));
+  memcpy(s->energy, save_energy, sizeof(save_energy));
+  free(save_acc);
+  return e;
+}
+
+/* Initialize of each integrator (SimulationEngine::DoStep's first call):
+ *   velocityverlet, verlet  UseOldConfig (one UpdateCell on the copy, then GoBack)
+ *   euler                   nothing (Integrator::Initialize)
+ *   leapfrog                UseOldConfig, UpdateForces(OldConfig), v_old += a_old 0.5 dt
+ *                           (plugins/leapfrog.cc:36-45)
+ *   beeman, nosehoover      UseOldConfig, UpdateForces(OldConfig); aux = 0, friction 0
+ *                           (plugins/beeman.cc:37-43, plugins/nosehoover.cc:35-42) */
+static int integ_initialize(orc_sim* s) {
+  if (s->integ == ORC_INT_EULER)
+    return ORC_OK;
+  int e = cm_update_cell(s);
+  if (e || s->integ == ORC_INT_VV)
+    return e;
+  if ((e = go_back(s)))
+    return e;
+  if (s->integ == ORC_INT_VERLET)
+    return ORC_OK;
+  double* a_old = (double*)malloc(sizeof(double) * 3 * (size_t)(s->n > 0 ? s->n : 1));
+  if (!a_old)
+    return ORC_ERR_NOMEM;
+  e = old_config_forces(s, a_old);
+  if (e == ORC_OK) {
+    for (int64_t k = 0; k < 3 * s->n; ++k) {
+      if (s->integ == ORC_INT_LEAPFROG) {
+        s->old_vel[k] += a_old[k] * 0.5 * s->dt;
+      } else {
+        s->old_acc[k] = a_old[k];
+        s->aux[k] = 0.0;
+      }
+    }
+    s->friction = 0.0;
+  }
+  free(a_old);
+  return e;
+}
+
+static int moves(const orc_sim* s, int64_t i) { return !(s->have_fixedpos && (s->flags[i] & ORC_FIXEDPOS)); }
+
+/* Euler::Advance (plugins/euler.cc:37-43), Leapfrog::Advance (plugins/leapfrog.cc:47-57),
+ * Verlet::Advance (plugins/verlet.cc:41-55); OneStepIntegrator::Advance around them
+ * (liblpmd/simulation/onestepintegrator.cc:13-40). */
+static int onestep_advance(orc_sim* s) {
+  int e = orc_sim_update_forces(s);
+  if (e)
+    return e;
+  zero_fixedvel(s);
+  const double dt = s->dt;
+  for (int64_t i = 0; i < s->n; ++i) {
+    if (!moves(s, i))
+      continue;
+    double* x = &s->pos[3 * i];
+    double* v = &s->vel[3 * i];
+    const double* a = &s->acc[3 * i];
+    double np[3];
+    if (s->integ == ORC_INT_EULER) {
+      for (int q = 0; q < 3; ++q)
+        np[q] = x[q] + v[q] * dt;
+      orc_fitted_inside(s->L, np, x);
+      for (int q = 0; q < 3; ++q)
+        v[q] += a[q] * dt;
+    } else if (s->integ == ORC_INT_LEAPFROG) {
+      double* ov = &s->old_vel[3 * i];
+      double vh[3];
+      for (int q = 0; q < 3; ++q) {
+        vh[q] = ov[q] + a[q] * dt;
+        np[q] = x[q] + vh[q] * dt;
+      }
+      orc_fitted_inside(s->L, np, x);
+      for (int q = 0; q < 3; ++q) {
+        v[q] = (vh[q] + ov[q]) * 0.5;
+        ov[q] = vh[q];
+      }
+    } else { /* verlet */
+      double* op = &s->old_pos[3 * i];
+      double oldpos[3];
+      for (int q = 0; q < 3; ++q) {
+        oldpos[q] = op[q];
+        np[q] = (x[q] * 2.0 - op[q]) + a[q] * dt * dt;
+        op[q] = x[q];
+        s->old_vel[3 * i + q] = v[q];
+      }
+      orc_fitted_inside(s->L, np, x);
+      double d[3];
+      orc_displacement(s->L, oldpos, x, d);
+      for (int q = 0; q < 3; ++q)
+        v[q] = d[q] / (2.0 * dt);
+    }
+  }
+  return ORC_OK;
+}
+
+/* Beeman (plugins/beeman.cc:45-70) and NoseHoover (plugins/nosehoover.cc:44-83) under
+ * TwoStepIntegrator::Advance.  Nose-Hoover adds its friction increment for every moving atom,
+ * in atom order, before that atom's update; the temperature is that of all atoms (tag false),
+ * the Boltzmann constant the session's 0.00008617 (liblpmd/runtime/session.cc:17-32). */
+static int twostep_advance(orc_sim* s) {
+  int e = orc_sim_update_forces(s);
+  if (e)
+    return e;
+  zero_fixedvel(s);
+  const double dt = s->dt;
+  double inc = 0.0;
+  if (s->integ == ORC_INT_NOSEHOOVER) {
+    double K = 0.0;
+    for (int64_t i = 0; i < s->n; ++i)
+      K += 0.5 * s->mass[i] * sqmod(&s->vel[3 * i]);
+    double T = (s->n == 0) ? 0.0 : (2.0 / 3.0) * (K * ORC_KIN2EV) / (ORC_KBOLTZMANN * (double)s->n);
+    inc = ((3.0 * (double)s->n / s->fmass) * 0.00008617 * (T - s->t0) * dt);
+  }
+  for (int64_t i = 0; i < s->n; ++i) {
+    if (!moves(s, i))
+      continue;
+    double* x = &s->pos[3 * i];
+    const double* v = &s->vel[3 * i];
+    double* a = &s->acc[3 * i];
+    double* oa = &s->old_acc[3 * i];
+    double na[3], np[3];
+    if (s->integ == ORC_INT_NOSEHOOVER) {
+      s->friction += inc;
+      for (int q = 0; q < 3; ++q) {
+        na[q] = a[q] - v[q] * s->friction;
+        a[q] = na[q];
+      }
+    } else {
+      for (int q = 0; q < 3; ++q)
+        na[q] = a[q];
+    }
+    for (int q = 0; q < 3; ++q) {
+      s->aux[3 * i + q] = oa[q];
+      np[q] = x[q] + v[q] * dt + na[q] * (2.0 / 3.0) * dt * dt - oa[q] * (1.0 / 6.0) * dt * dt;
+      oa[q] = na[q];
+    }
+    orc_fitted_inside(s->L, np, x);
+  }
+  e = orc_sim_update_forces(s);
+  if (e)
+    return e;
+  zero_fixedvel(s);
+  for (int64_t i = 0; i < s->n; ++i) {
+    if (!moves(s, i))
+      continue;
+    double* v = &s->vel[3 * i];
+    for (int q = 0; q < 3; ++q)
+      v[q] = v[q] + s->acc[3 * i + q] * (1.0 / 3.0) * dt + s->old_acc[3 * i + q] * (5.0 / 6.0) * dt -
+             s->aux[3 * i + q] * (1.0 / 6.0) * dt;
+  }
+  return ORC_OK;
+}
+
 /* KineticEnergy / Temperature / Momentum, liblpmd/lpmd/properties.h:22-81, and
  * SetSimulationTags, liblpmd/simulation/simulationbuilder.cc:84-124. */
 int orc_sim_thermo(const orc_sim* s, double* out) {
@@ -1283,12 +1500,14 @@ int orc_sim_do_steps(orc_sim* s, int64_t nsteps, double* thermo) {
       for (int b = 0; b < 3; ++b)
         s->stress[a][b] = 0.0;
     if (!s->initialized) {
-      int e = cm_update_cell(s);
+      int e = integ_initialize(s);
       if (e)
         return e;
       s->initialized = 1;
     }
-    int e = vv_advance(s);
+    int e = (s->integ == ORC_INT_VV) ? vv_advance(s)
+            : (s->integ == ORC_INT_BEEMAN || s->integ == ORC_INT_NOSEHOOVER) ? twostep_advance(s)
+                                                                           : onestep_advance(s);
     if (e)
       return e;
     s->step++;

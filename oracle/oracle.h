@@ -20,6 +20,8 @@
  *   - Gupta functionals                              plugins/gupta.cc:52-75
  *   - FastLJ tables and lookups                      plugins/fastlj.cc:38-73
  *   - LCBinary grid, growth and neighbour lists      plugins/lcbinary.cc:50-254
+ *   - Euler, Leapfrog, Verlet, Beeman, NoseHoover    plugins/euler.cc, leapfrog.cc, verlet.cc,
+ *                                                    beeman.cc, nosehoover.cc
  *   - CombinedPotential::UpdateForces                liblpmd/lpmd/combinedpotential.h:39-52
  *   - TwoStepIntegrator::Advance + VelocityVerlet    liblpmd/simulation/twostepintegrator.cc:12-68,
  *                                                    plugins/velocityverlet.cc:55-75,
@@ -108,6 +110,10 @@ int orc_sim_set_lcbinary(orc_sim* s, double cutoff, int nx, int ny, int nz, int 
 int orc_sim_add_potential(orc_sim* s, int kind, const double* params, int nparams, int s1, int s2);
 
 int orc_sim_set_velocityverlet(orc_sim* s, double dt);
+enum { ORC_INT_VV = 0, ORC_INT_EULER = 1, ORC_INT_LEAPFROG = 2, ORC_INT_VERLET = 3, ORC_INT_BEEMAN = 4,
+       ORC_INT_NOSEHOOVER = 5 };
+/* velocityverlet, euler, leapfrog, verlet, beeman, nosehoover (fmass, t: nosehoover only) */
+int orc_sim_set_integrator(orc_sim* s, int kind, double dt, double fmass, double t);
 
 /* CombinedPotential::UpdateForces: zero acc/virial/stress, UpdateCell, every potential. */
 int orc_sim_update_forces(orc_sim* s);

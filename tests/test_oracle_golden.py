@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import GOLDEN_CASES, load_golden, neighbor_hashes
+from helpers import GOLDEN_CASES, INTEG_CASES, load_golden, neighbor_hashes
 from lpmd2_gb300 import inputs as I
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
@@ -33,12 +33,13 @@ def _same(a, b, rtol=1e-12):
 def _replay(g):
     pots = [(str(n), str(a), int(s[0]), int(s[1]))
             for n, a, s in zip(g["pot_names"], g["pot_args"], g["pot_species"])]
+    integ = (str(g["integ_name"]), str(g["integ_args"])) if "integ_name" in g else None
     return oracle.run_port(g["pos_in"], g["L"], g["Z"], g["mass"], g["vel_in"], str(g["cm"]),
                            str(g["cm_args"]), pots, float(g["dt"]), int(g["nsteps"]),
-                           neigh=(bool(g["neigh_full"]), float(g["neigh_rcut"])))
+                           neigh=(bool(g["neigh_full"]), float(g["neigh_rcut"])), integrator=integ)
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("case", GOLDEN_CASES + INTEG_CASES)
 def test_port_matches_reference(case):
     g = load_golden(case)
     out = _replay(g)

@@ -52,6 +52,11 @@ class GBMDIntegrator : public Integrator, public Plugin {
     DefineKeyword("precision", "mixed");   // fp64 | mixed
     DefineKeyword("device", "0");
     DefineKeyword("sync-each", "1");       // copy the state back every n steps
+    // the integrator run on the GPU: velocityverlet | euler | leapfrog | verlet | beeman |
+    // nosehoover (the last with fmass and t, as the nosehoover plugin takes them)
+    DefineKeyword("scheme", "velocityverlet");
+    DefineKeyword("fmass", "0");
+    DefineKeyword("t", "300.0");
     ProcessArguments(args);
   }
   ~GBMDIntegrator() { if (sim) gbmd_sim_destroy(sim); }
@@ -94,7 +99,10 @@ class GBMDIntegrator : public Integrator, public Plugin {
       check(gbmd_sim_add_potential(sim, h, s1, s2));
       gbmd_plugin_destroy(h);
     }
-    check(gbmd_plugin_create("velocityverlet", ("dt " + (*this)["dt"]).c_str(), &h));
+    const std::string scheme = (*this)["scheme"];
+    std::string iargs = "dt " + (*this)["dt"];
+    if (scheme == "nosehoover") iargs += " fmass " + (*this)["fmass"] + " t " + (*this)["t"];
+    check(gbmd_plugin_create(scheme.c_str(), iargs.c_str(), &h));
     check(gbmd_sim_set_integrator(sim, h));
     gbmd_plugin_destroy(h);
     check(gbmd_sim_set_precision(sim, (*this)["precision"] == "fp64" ? GBMD_PRECISION_FP64
@@ -103,7 +111,7 @@ class GBMDIntegrator : public Integrator, public Plugin {
     pull(s);
   }
 
-  // One Simulation::DoStep: both force evaluations and both half-kicks on the GPU.
+  // One Simulation::DoStep on the GPU: the chosen integrator's force evaluations and updates.
   void Advance(Simulation& s, Potential&) override {
     check(gbmd_sim_do_steps(sim, 1));
     if (++since_sync >= int((*this)["sync-each"])) { pull(s); since_sync = 0; }

@@ -28,9 +28,13 @@ int main(int argc, char** argv) {
   lpmd::Plugin* p = lpmd::PluginLoader(argv[1], "dt 2.5 precision fp64");
   lpmd::Integrator* integ = dynamic_cast<lpmd::Integrator*>(p);
   lpmd::Plugin& q = *p;
-  std::printf("name=%s dt=%s precision=%s device=%s sync=%s integrator=%d\n", q.Name().c_str(),
+  std::printf("name=%s dt=%s precision=%s device=%s sync=%s scheme=%s integrator=%d\n", q.Name().c_str(),
               std::string(q["dt"]).c_str(), std::string(q["precision"]).c_str(),
-              std::string(q["device"]).c_str(), std::string(q["sync-each"]).c_str(), integ != nullptr);
+              std::string(q["device"]).c_str(), std::string(q["sync-each"]).c_str(),
+              std::string(q["scheme"]).c_str(), integ != nullptr);
+  lpmd::Plugin& nh = *lpmd::PluginLoader(argv[1], "scheme nosehoover fmass 1e9 t 120");
+  std::printf("scheme=%s fmass=%s t=%s\n", std::string(nh["scheme"]).c_str(), std::string(nh["fmass"]).c_str(),
+              std::string(nh["t"]).c_str());
   try {
     lpmd::PluginLoader(argv[1], "dt 1.0 device");
     std::printf("no error\n");
@@ -64,6 +68,7 @@ def test_plugin_loads_through_lpmd(plugin):
     env = dict(os.environ, LD_LIBRARY_PATH=f"{GBMD_LIB.parent}:{os.environ.get('LD_LIBRARY_PATH', '')}")
     out = subprocess.run([str(exe), str(so)], capture_output=True, text=True, env=env, timeout=60)
     assert out.returncode == 0, out.stderr
-    first, second = out.stdout.splitlines()[:2]
-    assert first == "name=gbmd dt=2.5 precision=fp64 device=0 sync=1 integrator=1"
+    first, nh, second = out.stdout.splitlines()[:3]
+    assert first == "name=gbmd dt=2.5 precision=fp64 device=0 sync=1 scheme=velocityverlet integrator=1"
+    assert nh == "scheme=nosehoover fmass=1e9 t=120"
     assert second.startswith("error:")

@@ -176,6 +176,17 @@ def _p(a, t=_D):
     return None if a is None else a.ctypes.data_as(t)
 
 
+def _out3(out, n):
+    if out is None:
+        return tuple(np.zeros((n, 3)) for _ in range(3))
+    if len(out) != 3:
+        raise ValueError("out: three (n, 3) arrays")
+    for x in out:
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.shape == (n, 3) and x.flags.c_contiguous):
+            raise ValueError("out arrays must be C-contiguous float64 of shape (n, 3)")
+    return tuple(out)
+
+
 def _vec(a, n):
     if a is None:
         return None
@@ -355,8 +366,11 @@ class Simulation:
         f = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
         _check(self.lib.gbmd_sim_set_flags(self.h, _p(f, _U8)))
 
-    def atoms(self):
-        p, v, a = (np.zeros((self.n, 3)) for _ in range(3))
+    def atoms(self, out=None):
+        """Positions, velocities, accelerations (n x 3, original atom order).  `out`: three
+        C-contiguous float64 (n, 3) arrays to fill instead (e.g. pinned host memory, which the
+        copies then reach by DMA without staging)."""
+        p, v, a = _out3(out, self.n)
         _check(self.lib.gbmd_sim_get_atoms(self.h, _p(p), _p(v), _p(a)))
         return p, v, a
 
@@ -478,9 +492,9 @@ class Batch:
         """Simulation.berendsen for one system (-1: every active system)."""
         _check(self.lib.gbmd_batch_scale_velocities(self.h, sys, 1, float(target), float(dt_over_tau)))
 
-    def atoms(self, sys: int):
+    def atoms(self, sys: int, out=None):
         n = int(self.natoms[sys])
-        p, v, a = (np.zeros((n, 3)) for _ in range(3))
+        p, v, a = _out3(out, n)
         _check(self.lib.gbmd_batch_get_atoms(self.h, sys, _p(p), _p(v), _p(a)))
         return p, v, a
 

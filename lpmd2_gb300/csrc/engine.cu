@@ -319,31 +319,35 @@ struct Engine::Impl {
       if (!any) return;
       k_binary_clear<<<1, 256, 0, s>>>(D);
       launched();
-      // new geometry for every system (cell bases move), then the same re-sort again
-      total_cells = 0;
-      for (int q = 0; q < nsys; ++q) {
-        SysDev& S = sysd[q];
-        for (int a = 0; a < 3; ++a) S.n[a] = lcb_n[q][a];
-        S.lc_side = lcb_side(S.L, S.n, cm.cutoff);
-        for (int a = 0; a < 3; ++a) {
-          S.d[a] = S.L[a] / (double)S.n[a];
-          S.df[a] = (float)S.d[a];
-          S.ninv[a] = (double)S.n[a] / S.L[a];
-        }
-        S.ncells = S.n[0] * S.n[1] * S.n[2];
-        S.cell_base = total_cells;
-        total_cells += S.ncells;
-      }
-      for (int a = 0; a < 3; ++a) st.cell_grid[a] = sysd[0].n[a];
-      free_cells();
-      alloc_cells(total_cells);
-      alloc_list(0);
-      upload_sysd();
-      k_cell_centres<<<nblocks(total_cells, 256), 256, 0, s>>>(D);
-      launched();
+      lcb_apply_grids(s);
       launch_rebuild_kernels(s);
     }
     throw Error(7, "lcbinary: no collision-free grid after 64 enlargements");
+  }
+
+  // New geometry for every system from lcb_n (cell bases move) and a fresh cell pool.
+  void lcb_apply_grids(cudaStream_t s) {
+    total_cells = 0;
+    for (int q = 0; q < nsys; ++q) {
+      SysDev& S = sysd[q];
+      for (int a = 0; a < 3; ++a) S.n[a] = lcb_n[q][a];
+      S.lc_side = lcb_side(S.L, S.n, cm.cutoff);
+      for (int a = 0; a < 3; ++a) {
+        S.d[a] = S.L[a] / (double)S.n[a];
+        S.df[a] = (float)S.d[a];
+        S.ninv[a] = (double)S.n[a] / S.L[a];
+      }
+      S.ncells = S.n[0] * S.n[1] * S.n[2];
+      S.cell_base = total_cells;
+      total_cells += S.ncells;
+    }
+    for (int a = 0; a < 3; ++a) st.cell_grid[a] = sysd[0].n[a];
+    free_cells();
+    alloc_cells(total_cells);
+    alloc_list(0);
+    upload_sysd();
+    k_cell_centres<<<nblocks(total_cells, 256), 256, 0, s>>>(D);
+    launched();
   }
 
   Dev D{};
@@ -1881,6 +1885,15 @@ void Engine::checkpoint_load(const void* buf, size_t bytes) {
   if (bytes != sizeof(CkptHeader) + h.body_bytes) throw Error(1, "checkpoint: size mismatch");
   if (h.natoms_total != I.N || h.nsys != I.nsys) throw Error(1, "checkpoint: different systems");
   I.ensure_ready();
+  if (h.total_cells != I.total_cells && I.lcb_exact() && h.config_hash == config_hash(I)) {
+    // lcbinary grids only grow: adopt the saved ones (their counts are in the saved systems)
+    std::vector<SysDev> saved(I.nsys);
+    if (bytes < sizeof(CkptHeader) + sizeof(SysDev) * I.nsys) throw Error(1, "checkpoint: truncated");
+    std::memcpy(saved.data(), (const char*)buf + sizeof(CkptHeader), sizeof(SysDev) * I.nsys);
+    for (int q = 0; q < I.nsys; ++q)
+      for (int a = 0; a < 3; ++a) I.lcb_n[q][a] = saved[q].n[a];
+    I.lcb_apply_grids(I.stream);
+  }
   if (h.config_hash != config_hash(I) || h.precision != I.precision || h.total_cells != I.total_cells)
     throw Error(1, "checkpoint: cell manager, potentials, integrator, precision or options differ");
   if (h.maxnb != I.D.maxnb) {  // the saved list had grown: give this engine the same capacity

@@ -101,3 +101,23 @@ def test_checkpoint_needs_the_same_configuration():
         b.restore(ck)
     with pytest.raises(gbmd.GbmdError, match="gbmd checkpoint|truncated|size"):
         b.restore(ck[:100])
+
+
+def test_lcbinary_checkpoint_after_the_grid_grew():
+    # lj_lcbinary_grow starts from a 4x4x4 sub-cell grid that grows until no sub-cell holds two
+    # atoms; a fresh simulation restoring the snapshot adopts the grown grid
+    g = load_golden("lj_lcbinary_grow")
+    a = make_sim(g, "fp64")
+    a.update_forces()
+    a.do_steps(7)
+    grown = a.stats()["cell_grid"]
+    assert min(grown) > 4
+    data = a.checkpoint()
+    a.do_steps(9)
+    want = state(a)
+    b = make_sim(g, "fp64")
+    b.restore(data)
+    assert b.stats()["cell_grid"] == grown
+    b.do_steps(9)
+    for x, y in zip(want, state(b)):
+        np.testing.assert_array_equal(x, y)

@@ -154,3 +154,51 @@ def test_input_from_an_lpmd_file(tmp_path):
     p, v, _ = sim.atoms()
     np.testing.assert_array_equal(out["pos"], p)
     np.testing.assert_array_equal(out["vel"], v)
+
+
+def test_control_file_with_sibling_plugins_matches_the_api(tmp_path):
+    # gupta + lcbinary + beeman from a control file = the same plugins through the API
+    text = """
+cell cubic 16.32
+input crystal3d type=fcc symbol=Au nx=4 ny=4 nz=4
+prepare temperature t=300.0 seed=3
+steps 25
+use gupta
+ A 0.2061
+ r0 2.884
+ p 10.229
+ B 1.790
+ q 4.036
+ cutoff 6.0
+enduse
+use lcbinary
+ cutoff 6.0
+ mode auto
+enduse
+use beeman
+ dt 2.0
+enduse
+potential gupta Au Au
+cellmanager lcbinary
+integrator beeman
+"""
+    ctl = C.parse(text, strict=True)
+    out = C.run(ctl, precision="fp64", workdir=tmp_path)
+    from lpmd2_gb300 import inputs as I
+
+    L = np.full(3, 16.32)
+    pos = C.crystal3d("fcc", 4, 4, 4, L)
+    n = len(pos)
+    mass = np.full(n, C.STANDARD_MASS["Au"])
+    vel = I.maxwell_boltzmann(mass, 300.0, seed=3)
+    sim = gbmd.Simulation(n, L)
+    sim.set_atoms(pos, vel, Z=np.full(n, 79, dtype=np.int32), mass=mass)
+    sim.set_cell_manager(gbmd.Plugin("lcbinary", "cutoff 6.0 mode auto"))
+    sim.add_potential(gbmd.Plugin("gupta", "A 0.2061 r0 2.884 p 10.229 B 1.790 q 4.036 cutoff 6.0"), 79, 79)
+    sim.set_integrator(gbmd.Plugin("beeman", "dt 2.0"))
+    sim.set_precision("fp64")
+    sim.update_forces()
+    sim.do_steps(25)
+    p, v, _ = sim.atoms()
+    np.testing.assert_array_equal(out["pos"], p)
+    np.testing.assert_array_equal(out["vel"], v)

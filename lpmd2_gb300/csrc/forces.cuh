@@ -742,6 +742,50 @@ __device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, in
   return waited;
 }
 
+// As warp_list_ring, two groups per iteration: both stages are read before either body runs,
+// so the two groups' neighbour gathers can be in flight together (for latency-bound bodies).
+template <class F>
+__device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
+                                                uint4 (*ring)[32], unsigned long long* bar, F&& body) {
+  const int lane = threadIdx.x & 31;
+  const uint4* src0 = list_group(D, S, wfirst, 0);
+  const unsigned bytes = (unsigned)wcount * 16u;
+  const int na = S.natoms;
+  if (lane == 0 && ngw > 0) {
+    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
+    mbar_init_fence();
+    for (int r = 0; r < RING && r < ngw; ++r) {
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
+    }
+  }
+  __syncwarp();
+  bool waited = true;
+  for (int q = 0; q < ngw; q += 2) {
+    const bool two = q + 1 < ngw;
+    const int r0 = q & (RING - 1), r1 = (q + 1) & (RING - 1);
+    if (!mbar_wait_bounded(&bar[r0], (unsigned)((q / RING) & 1))) waited = false;
+    if (two && !mbar_wait_bounded(&bar[r1], (unsigned)(((q + 1) / RING) & 1))) waited = false;
+    const uint4 c0 = ring[r0][lane];
+    const uint4 c1 = two ? ring[r1][lane] : make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();  // every lane has its entries: the stages can be refilled
+    if (lane == 0) {
+      fence_proxy_async_shared();
+      if (q + RING < ngw) {
+        mbar_expect_tx(&bar[r0], bytes);
+        bulk_g2s(ring[r0], src0 + (long long)(q + RING) * na, bytes, &bar[r0]);
+      }
+      if (two && q + 1 + RING < ngw) {
+        mbar_expect_tx(&bar[r1], bytes);
+        bulk_g2s(ring[r1], src0 + (long long)(q + 1 + RING) * na, bytes, &bar[r1]);
+      }
+    }
+    body(q, c0);
+    if (two) body(q + 1, c1);
+  }
+  return waited;
+}
+
 // Mixed density pass over the Verlet list: FP32 rho_ij of each group of four entries
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
@@ -791,7 +835,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
   const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
   const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
-  const bool waited = warp_list_ring(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], [&](int g, const uint4& e4) {
+  const bool waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], [&](int g, const uint4& e4) {
     if (g < ng) {
       const int rem = cnt - 4 * g;
       const float part = ((term(e4.x, true) + term(e4.y, rem > 1)) + term(e4.z, rem > 2)) + term(e4.w, rem > 3);

@@ -21,6 +21,7 @@ simulation it describes through libgbmd:
   output module=lpmd file=F [level= type=lpmd|zlp blocksize= compression= extra=TYPE]
                                                                lpmd / zlp frames (lpmd.cc)
   mass <symbol> <value>, set <option> <value>, periodic x y z
+  set restore-file F / dumping-each N / dumping-file F / lastconfig F   text dumps (Dump/Restore)
 
 Thermo comes from the device's per-step record, so monitored steps cost no extra
 synchronisation; positions are copied back only for the output frames.  Thermostats
@@ -238,7 +239,7 @@ def _kv(args: str) -> dict:
     return {w[k]: w[k + 1] for k in range(0, len(w) - 1, 2)}
 
 
-def modifier_schedule(ctl: Control, dt: float) -> list[tuple[int, int, float, float]]:
+def modifier_schedule(ctl: Control, dt: float, first_step: int = 0) -> list[tuple[int, int, float, float]]:
     """The velocity rescalings the applied modifiers make, as (step, mode, target T, dt/tau)
     after that step, in the order lpmd runs them (Application::RunModifiers after DoStep,
     lpmd/application.cc:403-464).  Stepper activity and the linear ramp follow
@@ -268,7 +269,7 @@ def modifier_schedule(ctl: Control, dt: float) -> list[tuple[int, int, float, fl
             return m["frm"]
         return m["frm"] + float(k - m["start"]) / float(m["end"] - m["start"]) * (m["to"] - m["frm"])
 
-    for k in range(1, ctl.steps + 1):
+    for k in range(first_step + 1, ctl.steps + 1):  # a restored run starts after its dump's step
         for m in mods:
             if not _active(k, m["start"], m["end"], m["each"]):
                 continue
@@ -324,7 +325,29 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         raise ControlError("the GPU path runs fully periodic cells only")
     inp = ctl.input or {}
     cell = np.asarray(ctl.cell, dtype=np.float64)
-    if inp.get("module") == "crystal3d":
+    step0 = 0
+    flags = None
+    restore = ctl.options.get("restore-file")
+    if restore:
+        # LPMD::RestoreSimulation -> Simulation::Restore (lpmd/lpmd.cc:32-50,
+        # liblpmd/simulation/simulationbuilder.cc:240-293): atoms, cell and step from a dump; no
+        # input module and no prepares (lpmd/application.cc:59); the run continues from the step
+        path = Path(restore)
+        path = path if path.is_absolute() else workdir / path
+        try:
+            d = F.read_dump(path)
+        except (OSError, ValueError, IndexError) as e:
+            raise ControlError(f"restore-file: {e}") from None
+        cell = np.asarray(d["L"], dtype=np.float64)
+        pos, vel, Z = d["pos"], d["vel"], d["Z"]
+        n = len(pos)
+        syms = [_SYMBOLS[int(z) - 1] for z in Z]
+        table = {sy: _species(sy, ctl) for sy in set(syms)}
+        masses = np.array([table[sy][1] for sy in syms])
+        symbols = syms[0] if len(table) == 1 else syms
+        step0 = d["step"]
+        flags = d["flags"] if d["flags"].any() else None
+    elif inp.get("module") == "crystal3d":
         symbols = inp.get("symbol", "H")
         Z, mass = _species(symbols, ctl)
         pos = crystal3d(inp.get("type", "fcc"), int(inp.get("nx", 1)), int(inp.get("ny", 1)), int(inp.get("nz", 1)),
@@ -353,7 +376,7 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         symbols = fr["symbols"][0] if len(table) == 1 else fr["symbols"]
     else:
         raise ControlError("input: the crystal3d generator and lpmd/zlp/xyz files run on the GPU path")
-    for pr in ctl.prepares:
+    for pr in ([] if restore else ctl.prepares):
         if pr.get("module") != "temperature":
             raise ControlError(f"prepare {pr.get('module')}: not supported on the GPU path")
         vel = I.maxwell_boltzmann(masses, float(pr.get("t", "0")), seed=int(pr.get("seed", "1")))
@@ -372,6 +395,8 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         raise ControlError("MissingComponent: integrator")
     sim = gbmd.Simulation(n, cell, device=device)
     sim.set_atoms(pos, vel, Z=Z, mass=masses)
+    if flags is not None:
+        sim.set_flags(flags)
     sim.set_cell_manager(plugin(ctl.cellmanager, "cellmanager"))
     for uid, a, b in ctl.potentials:
         s1 = -1 if a == "all" else ATOMIC_NUMBER[a]
@@ -406,11 +431,22 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         w.write_frame(symbols, cell, p, v, a)
 
     dt = float(_kv(ctl.uses[ctl.integrator][1]).get("dt", "1.0"))
-    schedule = modifier_schedule(ctl, dt)
+    schedule = modifier_schedule(ctl, dt, first_step=step0)
     by_step: dict[int, list] = {}
     for st_, mode, target, dtt in schedule:
         by_step.setdefault(st_, []).append((mode, target, dtt))
-    done = 0
+    # Simulation::Dump every `dumping-each` steps into `dumping-file`, and into `lastconfig` at
+    # the end (lpmd/lpmd.cc:84-104; lastconfig defaults to lastconfig.dump, controlparser.cc:56)
+    dump_each = int(ctl.options.get("dumping-each", "0") or 0)
+    dump_file = ctl.options.get("dumping-file", "dump.dump")
+    last_file = ctl.options.get("lastconfig", "lastconfig.dump")
+    dump_steps = {t for t in range(step0 + 1, ctl.steps + 1) if _active(t, 0, ctl.steps, dump_each)} if dump_each > 0 else set()
+
+    def dump(name: str, step: int):
+        p_, v_, a_ = sim.atoms()
+        F.write_dump(workdir / name, step, cell, Z if np.ndim(Z) else np.full(n, Z), p_, v_, a_, flags)
+
+    done = step0
     while done < ctl.steps:
         # run to the next output frame, modifier or full thermo log, then report the chunk
         k = min(ctl.steps - done, 1000)
@@ -419,7 +455,7 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
                 if _active(s, st, en, ev):
                     k = s - done
                     break
-        nxt = [t for t in by_step if done < t <= done + k]
+        nxt = [t for t in by_step if done < t <= done + k] + [t for t in dump_steps if done < t <= done + k]
         if nxt:
             k = min(nxt) - done
         sim.do_steps(k)
@@ -433,6 +469,8 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
                 sim.berendsen(target, dtt)
         log = sim.thermo_log()
         for rec in log:
+            rec = rec.copy()
+            rec[0] += step0  # the device counts the steps of this run
             step = int(round(rec[0]))
             tags = None
             for props, st, en, ev, stream in monitors:
@@ -448,6 +486,9 @@ def run(ctl: Control, device: int = 0, precision: str | None = None, out: TextIO
         for f, st, en, ev, lv in outputs:
             if _active(done, st, en, ev):
                 emit_frame(f, lv)
+        if done in dump_steps:
+            dump(dump_file, done)
+    dump(last_file, done)
     for *_, stream in monitors:
         if stream is not out:
             stream.close()

@@ -14,8 +14,13 @@ Writers produce the bytes of the reference's own output plugins for orthogonal c
         size as the reference stores it on LP64 little-endian hosts (htonl of the 32-bit size
         in an 8-byte word: 4 big-endian bytes, then 4 zero bytes).  The header says "LPMD 2.0 Z".
 
-Values are C-formatted ("%.6f" / "%.8f"), which rounds exactly as iostream's fixed notation
-does.  Readers accept what the writers (and the reference) write: xyz frames, and lpmd/zlp
+  dump  Simulation::Dump / Restore (liblpmd/simulation/simulationbuilder.cc:195-293), the text
+        checkpoint behind `lastconfig`, `dumping-each` and `restore-file`: the step, the cell
+        vectors, "Z x y z vx vy vz ax ay az " per atom in iostream's default notation (6
+        significant digits), then a colour line ("false ") and a tag line per atom.
+
+Values are C-formatted ("%.6f" / "%.8f" / "%g"), which rounds exactly as iostream's fixed and
+default notations do.  Readers accept what the writers (and the reference) write: xyz frames, and lpmd/zlp
 version 2.0 files (LPMDFormat::ReadHeader / ReadCell, plugins/lpmd.cc:125-430) with their
 HDR column list.  The reference's legacy 1.0 and binary-header "Z4L2P" variants are not read.
 """
@@ -251,3 +256,66 @@ def read_xyz(path) -> list[dict]:
                            level=(width - 4) // 3))
         k += 2 + n
     return frames
+
+
+# ----------------------------------------------------------------------------------------------
+# Simulation::Dump / Restore text (lossy: 6 significant digits)
+# ----------------------------------------------------------------------------------------------
+
+
+def _g(x: float) -> str:
+    """iostream's default notation (precision 6) of a double: C's %g."""
+    return "%g" % x
+
+
+def write_dump(path, step: int, L, Z, pos, vel, acc, flags=None) -> None:
+    """Simulation::Dump (liblpmd/simulation/simulationbuilder.cc:195-238) of an orthogonal cell.
+    flags (GBMD_FLAG_*: 1 fixedvel, 2 fixedpos) become the atoms' tags with value "true"."""
+    L = np.asarray(L, dtype=np.float64).reshape(3)
+    Z = np.asarray(Z).reshape(-1)
+    n = len(Z)
+    pos, vel, acc = (np.asarray(a, dtype=np.float64).reshape(n, 3) for a in (pos, vel, acc))
+    out = [f"{int(step)}\n"]
+    for i in range(3):
+        out.append("".join(_g(L[i] if q == i else 0.0) + " " for q in range(3)) + "\n")
+    out.append(f"{n}\n")
+    fmt = "%d " + "%g " * 9 + "\n"
+    data = np.hstack([pos, vel, acc])
+    out.extend(fmt % ((int(z),) + tuple(r)) for z, r in zip(Z, data))
+    out.append("false \n" * n)
+    for i in range(n):
+        f = 0 if flags is None else int(flags[i])
+        tags = sorted(t for bit, t in ((1, "fixedvel"), (2, "fixedpos")) if f & bit)  # tag keys in key order
+        out.append(f"{len(tags)} " + "".join(f"{t} true " for t in tags) + "\n")
+    Path(path).write_text("".join(out))
+
+
+def read_dump(path) -> dict:
+    """Simulation::Restore (liblpmd/simulation/simulationbuilder.cc:240-293): step, cell vectors,
+    atoms (Z, positions, velocities, accelerations) and the fixedvel / fixedpos tags as flags."""
+    w = Path(path).read_text().split()
+    k = 0
+    step = int(w[k]); k += 1
+    cell = np.array([float(x) for x in w[k:k + 9]]).reshape(3, 3); k += 9
+    n = int(w[k]); k += 1
+    Z = np.zeros(n, dtype=np.int32)
+    data = np.zeros((n, 9))
+    for i in range(n):
+        Z[i] = int(w[k])
+        data[i] = [float(x) for x in w[k + 1:k + 10]]
+        k += 10
+    for i in range(n):
+        have = w[k] == "true"
+        k += 4 if have else 1
+    flags = np.zeros(n, dtype=np.uint8)
+    for i in range(n):
+        m = int(w[k]); k += 1
+        for _ in range(m):
+            key, val = w[k], w[k + 1]
+            k += 2
+            if key == "fixedvel":
+                flags[i] |= 1
+            elif key == "fixedpos" and val == "true":
+                flags[i] |= 2
+    return dict(step=step, cell=cell, L=np.sqrt((cell ** 2).sum(axis=1)), Z=Z, pos=data[:, 0:3], vel=data[:, 3:6],
+                acc=data[:, 6:9], flags=flags)

@@ -339,6 +339,20 @@ def run_reference(pos, L, symbol, vel, cm, cm_args, pots, dt, nsteps, neigh=None
     return out
 
 
+def write_reference_dump(path, L, Z, pos, vel, acc, flags=None) -> None:
+    """Simulation::Dump of the reference (see ref_driver.cpp) for these atoms at step 0."""
+    lib = _ref()
+    n = len(pos)
+    arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (L, pos, vel, acc)]
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
+    rc = lib.ref_dump(ctypes.c_int64(n), _ptr(arr[0]), _ptr(Z, ctypes.POINTER(ctypes.c_int32)), _ptr(arr[1]),
+                      _ptr(arr[2]), _ptr(arr[3]), None if fl is None else fl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                      str(path).encode())
+    if rc:
+        raise OracleError("reference: " + lib.ref_last_error().decode())
+
+
 def write_reference_frames(path, module: str, args: str, L, Z, pos, vel=None, acc=None) -> None:
     """Writes frames [nframes, n, 3] through the reference's own output plugin (lpmd / xyz,
     see ref_driver.cpp); `args` must name `path` with its `file` keyword."""

@@ -282,3 +282,32 @@ extern "C" int ref_write_frames(int64_t n, const double* L, const int32_t* Z, in
     return 1;
   }
 }
+
+// Simulation::Dump (liblpmd/simulation/simulationbuilder.cc:195-238) of n atoms at step 0:
+// Z, positions, velocities, accelerations; flags[i] & 1 tags the atom fixedvel, & 2 fixedpos.
+extern "C" int ref_dump(int64_t n, const double* L, const int32_t* Z, const double* pos, const double* vel,
+                        const double* acc, const uint8_t* flags, const char* path) {
+  g_error[0] = 0;
+  try {
+    static RuntimeContext context;
+    Simulation& md = SimulationBuilder::CreateFixedOrthogonal(context, long(n), Atom("H"));
+    BasicCell& cell = md.Cell();
+    cell[0] = L[0] * e1;
+    cell[1] = L[1] * e2;
+    cell[2] = L[2] * e3;
+    BasicParticleSet& atoms = md.Atoms();
+    for (long i = 0; i < atoms.Size(); ++i) {
+      atoms[i].Z() = Z[i];
+      atoms[i].Position() = Vector(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+      atoms[i].Velocity() = Vector(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+      atoms[i].Acceleration() = Vector(acc[3 * i], acc[3 * i + 1], acc[3 * i + 2]);
+      if (flags && (flags[i] & 1)) atoms.SetTag(atoms[i], Tag("fixedvel"), "true");
+      if (flags && (flags[i] & 2)) atoms.SetTag(atoms[i], Tag("fixedpos"), "true");
+    }
+    md.Dump(path);
+    return 0;
+  } catch (std::exception& e) {
+    std::snprintf(g_error, sizeof g_error, "%s", e.what());
+    return 1;
+  }
+}

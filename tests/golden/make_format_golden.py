@@ -4,7 +4,8 @@ plugins (plugins/lpmd.cc LPMDFormat, plugins/xyz.cc XYZFormat), compiled into or
 
 inputs.npz holds the exact frames (two species, three frames, values that sit exactly on a
 rounding tie of the printed digit count, negative zeros and tiny negatives); each other file is
-the reference's output for one (module, arguments) case in CASES.
+the reference's output for one (module, arguments) case in CASES, and frame0.dump is the
+reference's Simulation::Dump of the first frame with some atoms tagged fixedvel / fixedpos.
 
 Usage:  python tests/golden/make_format_golden.py
 """
@@ -57,7 +58,15 @@ def main() -> None:
         oracle.build()
     OUT.mkdir(exist_ok=True)
     L, Z, pos, vel, acc = frames()
-    np.savez_compressed(OUT / "inputs.npz", L=L, Z=Z, pos=pos, vel=vel, acc=acc)
+    flags = np.zeros(len(Z), dtype=np.uint8)
+    flags[5], flags[7], flags[11] = 1, 2, 3
+    # %g edge cases: large / small magnitudes, exact ties of the 6th digit, negative zero
+    acc = acc.copy()
+    acc[0, 1] = [1.5e-12, -2.5e7, 123456.5]
+    acc[0, 2] = [-0.0, 1.0000005, 9.9999995e-5]
+    np.savez_compressed(OUT / "inputs.npz", L=L, Z=Z, pos=pos, vel=vel, acc=acc, flags=flags)
+    oracle.write_reference_dump(OUT / "frame0.dump", L, Z, pos[0], vel[0], acc[0], flags)
+    print(f"frame0.dump: {(OUT / 'frame0.dump').stat().st_size} bytes")
     for name, (module, args) in CASES.items():
         path = OUT / name
         oracle.write_reference_frames(path, module, f"file {path} {args}", L, Z, pos, vel, acc)

@@ -130,3 +130,17 @@ def test_one_symbol_for_all_atoms_writes_what_a_symbol_list_writes(module, name,
     assert a == b
     got = F.read_lpmd(tmp_path / ("a_" + name)) if module == "lpmd" else F.read_xyz(tmp_path / ("a_" + name))
     assert [fr["natoms"] for fr in got] == [n] * 3 and got[0]["symbols"] == ["Kr"] * n
+
+
+def test_dump_bytes_match_reference_and_read_back(tmp_path):
+    # Simulation::Dump of the reference (tests/golden/formats/frame0.dump): the first frame with
+    # atoms 5 / 7 / 11 tagged fixedvel / fixedpos / both, and %g edge values in the accelerations
+    g = np.load(GOLD / "inputs.npz")
+    F.write_dump(tmp_path / "d.dump", 0, g["L"], g["Z"], g["pos"][0], g["vel"][0], g["acc"][0], g["flags"])
+    assert (tmp_path / "d.dump").read_bytes() == (GOLD / "frame0.dump").read_bytes()
+    d = F.read_dump(GOLD / "frame0.dump")
+    assert d["step"] == 0 and list(d["Z"]) == list(g["Z"])
+    np.testing.assert_array_equal(d["L"], g["L"])
+    np.testing.assert_array_equal(d["flags"], g["flags"])
+    for key in ("pos", "vel", "acc"):
+        np.testing.assert_allclose(d[key], g[key][0], rtol=5e-6, atol=1e-300)

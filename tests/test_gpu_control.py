@@ -202,3 +202,36 @@ integrator beeman
     p, v, _ = sim.atoms()
     np.testing.assert_array_equal(out["pos"], p)
     np.testing.assert_array_equal(out["vel"], v)
+
+
+def test_dump_restore_continues_from_the_dumped_step(tmp_path):
+    from lpmd2_gb300 import formats as F
+
+    g = load_golden("lj_config1")
+    L = float(np.asarray(g["L"])[0])
+    base = control_text(L).replace("steps 100", "steps 20").replace("output xyz last.xyz each=100 level=1\n", "")
+    base = base.replace("monitor step,potential-energy,kinetic-energy,temperature each=1 output=monitor.dat",
+                        "monitor step,temperature each=1 output=monitor.dat")
+    first = C.run(C.parse(base + "set dumping-each 8\nset dumping-file every8.dump\n", strict=True),
+                  precision="fp64", workdir=tmp_path)
+    d = F.read_dump(tmp_path / "lastconfig.dump")
+    assert d["step"] == 20
+    np.testing.assert_allclose(d["pos"], first["pos"], rtol=5e-6)
+    assert F.read_dump(tmp_path / "every8.dump")["step"] == 16  # Stepper(0, 20, 8): 8, 16
+    # a second control file restores the dump and runs on to step 35
+    second = base.replace("steps 20", "steps 35") + "set restore-file lastconfig.dump\nset lastconfig final.dump\n"
+    out = C.run(C.parse(second, strict=True), precision="fp64", workdir=tmp_path)
+    rows = np.loadtxt(tmp_path / "monitor.dat")
+    assert list(rows[:, 0]) == list(range(21, 36))
+    assert F.read_dump(tmp_path / "final.dump")["step"] == 35
+    sim = gbmd.Simulation(len(d["pos"]), d["L"])
+    sim.set_atoms(d["pos"], d["vel"], Z=d["Z"], mass=g["mass"])
+    sim.set_cell_manager(gbmd.Plugin("linkedcell", "cutoff 8.5 nx 6 ny 6 nz 6"))
+    sim.add_potential(gbmd.Plugin("lennardjones", "sigma 3.405 epsilon 0.0103 cutoff 8.5"), 18, 18)
+    sim.set_integrator(gbmd.Plugin("velocityverlet", "dt 1.0"))
+    sim.set_precision("fp64")
+    sim.update_forces()
+    sim.do_steps(15)
+    p, v, _ = sim.atoms()
+    np.testing.assert_array_equal(out["pos"], p)
+    np.testing.assert_array_equal(out["vel"], v)

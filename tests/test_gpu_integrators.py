@@ -138,3 +138,37 @@ def test_switching_back_to_velocityverlet():
     th = sim.thermo_log()
     assert th.shape == (10, 22) and np.isfinite(th).all()
     np.testing.assert_array_equal(th[:, 0], np.arange(1, 11))
+
+
+@pytest.mark.parametrize("name", ["beeman", "nosehoover", "leapfrog"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_systems_match_their_runs_alone(name, precision):
+    # per-system history, Nose-Hoover friction and ranks: a batch of two liquids under the
+    # integrator gives each system the trajectory it has alone, bit for bit
+    from lpmd2_gb300 import inputs as I
+
+    systems = [I.lj_system(4, 0.85, 1.3, seed=91), I.lj_system(5, 0.8, 1.0, seed=92)]
+    sigma = I.LJ_AR["sigma"]
+    rc = 2.5 * sigma
+    args = "dt 5.0" + (" fmass 1e9 t 100" if name == "nosehoover" else "")
+
+    def setup(obj):
+        obj.set_cell_manager(gbmd.Plugin("verletlist", f"cutoff {rc!r} skin {0.3 * sigma!r} maxneighbors 256"))
+        obj.add_potential(gbmd.Plugin("lennardjones", f"sigma {sigma} epsilon {I.LJ_AR['epsilon']} cutoff {rc!r}"))
+        obj.set_integrator(gbmd.Plugin(name, args))
+        obj.set_precision(precision)
+        obj.update_forces()
+        obj.do_steps(23)
+
+    b = gbmd.Batch([s["natoms"] for s in systems], [s["L"] for s in systems])
+    for k, s in enumerate(systems):
+        b.set_atoms(k, s["pos"], s["vel"], Z=s["Z"], mass=s["mass"])
+    setup(b)
+    for k, s in enumerate(systems):
+        alone = gbmd.Batch([s["natoms"]], [s["L"]])
+        alone.set_atoms(0, s["pos"], s["vel"], Z=s["Z"], mass=s["mass"])
+        setup(alone)
+        for x, y in zip(b.atoms(k), alone.atoms(0)):
+            np.testing.assert_array_equal(x, y)
+        alone.close()
+    b.close()

@@ -235,3 +235,15 @@ def test_dump_restore_continues_from_the_dumped_step(tmp_path):
     p, v, _ = sim.atoms()
     np.testing.assert_array_equal(out["pos"], p)
     np.testing.assert_array_equal(out["vel"], v)
+
+
+@pytest.mark.parametrize("name", ["argon_liquid.control", "copper_thermostat.control"])
+def test_example_control_files_run(name, tmp_path):
+    from pathlib import Path
+
+    text = (Path(__file__).resolve().parents[1] / "examples" / name).read_text()
+    text = "\n".join("steps 60" if ln.startswith("steps ") else ln for ln in text.splitlines())
+    ctl = C.parse(text, strict=True)
+    out = C.run(ctl, workdir=tmp_path)
+    assert np.isfinite(out["pos"]).all() and np.isfinite(out["thermo"]["total_energy"])
+    assert (tmp_path / ctl.options.get("lastconfig", "lastconfig.dump")).exists()

@@ -16,6 +16,7 @@ import argparse
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -141,6 +142,29 @@ def allmax(dist, v: float) -> float:
     return float(t.item())
 
 
+def cpu_model() -> str:
+    """The host CPU's name (lscpu, else /proc/cpuinfo; Arm parts by their part number)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        info = Path("/proc/cpuinfo").read_text()
+        for line in info.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+        parts = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd0c": "Neoverse-N1"}
+        for line in info.splitlines():
+            if line.startswith("CPU part"):
+                return parts.get(line.split(":", 1)[1].strip(), "Arm part " + line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def cpu_sample(seconds_target: float = 15.0, procs: int | None = None) -> dict:
     """Times the reference CPU algorithm (oracle/_ref where built, else the C restatement) on
     a bounded sample: a 4,000-atom cut of the same liquid (FCC 10^3 at rho* 0.8442, T* 1.5,
@@ -155,10 +179,14 @@ def cpu_sample(seconds_target: float = 15.0, procs: int | None = None) -> dict:
     atoms = res[0][1]
     wall = max(r[2] for r in res)
     kind = res[0][3]
+    # (i) one process on one core, next to (ii) one replica per core above
+    with ctx.Pool(1) as pool:
+        one = pool.map(_cpu_worker, [seconds_target / 2])[0]
     return {"value": steps * atoms / wall, "unit": "atom-steps/s", "cores": ncores, "kind": kind,
+            "single_core_value": one[0] * one[1] / one[2], "cpu_model": cpu_model(),
             "sample": f"{ncores} replicas x {steps // ncores} steps of a {atoms}-atom cut of the liquid "
                       f"(FCC 10^3, linkedcell nx 4, velocityverlet, 2 force evaluations per step as the "
-                      f"reference does), {wall:.1f} s"}
+                      f"reference does), {wall:.1f} s; single_core_value: one process on one core"}
 
 
 def _cpu_worker(budget: float):
@@ -206,7 +234,8 @@ def run_reference_arm(args):
         "config": {"workload": "lj_liquid_fcc40_256k", "natoms": w["natoms"], "precision": "fp64",
                    "sampled_as": cb["sample"]},
         "cpu_baseline": {"value": cb["value"], "unit": cb["unit"], "cores": cb["cores"], "kind": cb["kind"],
-                         "sample": cb["sample"]},
+                         "sample": cb["sample"], "single_core_value": cb["single_core_value"],
+                         "cpu_model": cb["cpu_model"]},
         "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }

@@ -383,7 +383,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": "lj_liquid_fcc40_256k", "natoms": N, "rho_star": RHO_STAR, "T_star": T_STAR,
                    "cutoff_sigma": 2.5, "skin_sigma": 0.3, "dt_fs": w["dt"], "precision": "mixed",
-                   "graph_block": GRAPH_BLOCK, "melt_steps": args.melt,
+                   "graph_block": GRAPH_BLOCK, "melt_steps": args.melt, "seed": 2,
+                   "rng": "SplitMix64 (lpmd2_gb300/inputs.py)",
                    "l2": "flushed (256 MB write) before every 10-step graph block, outside the timing",
                    "parallelism": f"replicas x{world}"},
         "ns_per_day": value / N / world * w["dt"] * 86400 * 1e-6,
@@ -405,6 +406,7 @@ def main():
                      "peak_source": peak_kind},
         "step_roofline": {"achieved": step_achieved, "peak": peak, "unit": "GB/s", "frac": step_achieved / peak,
                           "bytes_per_atom_step": step_bytes_per_atom},
+        "flop_roofline": flop_roofline(value / world, RHO_STAR, clk.summary()),
         "kernel_ms": kt,
         "e2e": e2e,
         "clocks": clk.summary(),
@@ -477,6 +479,24 @@ def end_to_end(w, device: int, chunk: int = 100, reps: int = 3) -> dict:
     return {"value": N * chunk / t, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / chunk,
             "d2h_bytes_per_step": d2h / chunk, "chunk_steps": chunk,
             "note": "per chunk: set_atoms from pinned host arrays, UpdateForces, 100 steps, thermo log and state read back into pinned host arrays"}
+
+
+# Secondary, compute-side roofline of the LJ step: about 30 flops per pair evaluation and, with
+# full lists, (4/3) pi (rc/sigma)^3 rho* pair evaluations inside the cutoff per atom-step; the
+# peak is the nominal FP32 CUDA-core rate at the SM clock measured during the timed region.
+LJ_FLOPS_PER_PAIR = 30
+FP32_LANES_PER_SM = 128
+NUM_SMS = 152
+
+
+def flop_roofline(atom_steps_per_s: float, rho_star: float, clocks: dict) -> dict:
+    pairs = 4.0 / 3.0 * math.pi * 2.5 ** 3 * rho_star
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak = NUM_SMS * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12
+    achieved = atom_steps_per_s * pairs * LJ_FLOPS_PER_PAIR / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "flops_per_pair": LJ_FLOPS_PER_PAIR, "pairs_per_atom_step": pairs,
+            "peak_source": f"nominal FP32: {NUM_SMS} SMs x {FP32_LANES_PER_SM} lanes x 2 flop x {mhz:.0f} MHz"}
 
 
 def profiled_traffic(name: str):
@@ -602,7 +622,7 @@ def batched_ensemble(device: int, steps: int, nsys: int = 512, rank: int = 0, wo
     ms, ms64 = allmax(dist, ms), allmax(dist, ms64)
     value = total_atoms * steps / (ms * 1e-3)
     value64 = total_atoms * k64 / (ms64 * 1e-3)
-    return {"workload": f"lj_ensemble_{nsys}", "systems": nsys, "natoms_total": total_atoms,
+    return {"workload": f"lj_ensemble_{nsys}", "seed": 4, "systems": nsys, "natoms_total": total_atoms,
             "systems_this_rank": len(systems), "natoms_this_rank": natoms,
             "natoms_min": min(s["natoms"] for s in everything), "natoms_max": max(s["natoms"] for s in everything),
             "steps": steps, "value": value, "unit": "atom-steps/s", "ms_per_step": ms / steps,
@@ -634,7 +654,7 @@ def served_stream(device: int, njobs: int, rate: float, rank: int = 0, world: in
         res = [JobResult(0, "", n, st, a, finished=f, error=e) for part in gathered for (n, st, a, f, e) in part]
         wall = allmax(dist, wall)
     out = summarize(res, wall)
-    out.update({"rate_jobs_per_s": rate, "budget_bytes": 150e9, "batches": srv.batches_started,
+    out.update({"rate_jobs_per_s": rate, "seed": 5, "budget_bytes": 150e9, "batches": srv.batches_started,
                 "peak_budget_used_bytes": srv.peak_used,
                 "note": "latency = completion - arrival, wall clock; payloads generated before the clock starts"})
     return out
@@ -693,7 +713,7 @@ def eam_metal(device: int, steps: int, ncell: int = 50) -> dict:
     ms64 = time_batch(s64, device, GRAPH_BLOCK, k64)
     s64.close()
     value, value64 = N * steps / (ms * 1e-3), N * k64 / (ms64 * 1e-3)
-    return {"workload": "sc_cu_fcc50_vac1pct", "natoms": N, "steps": steps, "value": value, "unit": "atom-steps/s",
+    return {"workload": "sc_cu_fcc50_vac1pct", "seed": 3, "natoms": N, "steps": steps, "value": value, "unit": "atom-steps/s",
             "ms_per_step": ms / steps, "ns_per_day": value / N * 2.0 * 86400 * 1e-6, "fp64_value": value64,
             "speedup_vs_fp64": value / value64, "force_rms_rel_err_vs_fp64": frel,
             "epot_rel_err_vs_fp64": abs(tm["potential_energy"] - t64["potential_energy"]) / abs(t64["potential_energy"]),

@@ -254,7 +254,7 @@ def main():
                     help="short direct-launch run of the workload for ncu (no timing, no JSON)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
     ap.add_argument("--workload", default="lj", choices=["lj", "eam"], help="with --profile")
-    ap.add_argument("--drift-steps", type=int, default=2000, help="NVE steps of the drift comparison")
+    ap.add_argument("--drift-steps", type=int, default=10000, help="NVE steps of the drift comparison")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched ensemble (0: skip)")
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=32, help="jobs of the served stream (0: skip)")

@@ -1,4 +1,4 @@
-"""Python access to the checker: the C restatement (liboracle.so) and, where the reference
+"""Python access to the oracle: the C restatement (liboracle.so) and, where the reference
 sources were compiled here, the reference itself (_ref/libref_driver.so).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and the CPU-baseline

@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of LPMD's short-range MD timestep (see oracle.h).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for libgbmd, never part of the product path.
+ * TEST INFRASTRUCTURE ONLY: the oracle for libgbmd, never part of the product path.
  *
  * Every function names the reference lines it follows.  Arithmetic is written in the
  * reference's evaluation order (C++ left-to-right for chained * and +), and the file is

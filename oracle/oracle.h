@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of LPMD's short-range MD timestep.
  *
- * TEST INFRASTRUCTURE ONLY.  This code is the checker for the GPU library: it is
+ * TEST INFRASTRUCTURE ONLY.  This code is the oracle for the GPU library: it is
  * loaded by the tests, by __graft_entry__.smoke() and by the CPU-baseline leg of
  * bench.py, and by nothing else.  The product path (libgbmd) never links or calls it.
  *

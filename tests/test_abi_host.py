@@ -83,7 +83,7 @@ def test_plugin_errors():
 
 
 def _two_atom_force(name, args, r, mass=39.948):
-    """Force on atom 0 from atom 1 at distance r along x, from the checker (acc * m / ff)."""
+    """Force on atom 0 from atom 1 at distance r along x, from the oracle (acc * m / ff)."""
     L = [60.0, 60.0, 60.0]
     pos = np.array([[10.0, 10.0, 10.0], [10.0 + r, 10.0, 10.0]])
     out = oracle.run_port(pos, L, [1, 1], [mass, mass], None, "minimumimage", "cutoff 20",
@@ -92,7 +92,7 @@ def _two_atom_force(name, args, r, mass=39.948):
 
 
 @pytest.mark.parametrize("r", [3.2, 3.8, 5.0, 8.4])
-def test_lj_functionals_match_checker(r):
+def test_lj_functionals_match_oracle(r):
     p = gbmd.Plugin("lennardjones", LJ_AR)
     f, e = _two_atom_force("lennardjones", LJ_AR, r)
     assert p.pair_energy(r) == pytest.approx(e, rel=1e-14)
@@ -102,7 +102,7 @@ def test_lj_functionals_match_checker(r):
 @pytest.mark.parametrize("spec", [("suttonchen", SC_CU, 2.6), ("suttonchen", SC_CU, 5.1),
                                   ("finnissinclair", FS_FE, 2.5), ("finnissinclair-ext", FSX_MO, 2.9),
                                   ("gupta", GUPTA_AU, 2.7), ("gupta", GUPTA_AU, 4.9)])
-def test_metal_functionals_match_checker(spec):
+def test_metal_functionals_match_oracle(spec):
     name, args, r = spec
     p = gbmd.Plugin(name, args)
     f, e = _two_atom_force(name, args, r)

@@ -194,7 +194,7 @@ def test_cell_sort_matches_reference_order():
     np.testing.assert_array_equal(order, np.lexsort((np.arange(len(pos)), want)))
 
 
-def test_fixed_flags_match_checker():
+def test_fixed_flags_match_oracle():
     g = load_golden("lj_config1")
     n = len(g["pos_in"])
     flags = np.zeros(n, dtype=np.uint8)
@@ -214,7 +214,7 @@ def test_fixed_flags_match_checker():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_species_filter_matches_checker(precision):
+def test_species_filter_matches_oracle(precision):
     """Potential::AppliesTo (liblpmd/simulation/potential.cc:25-27) with two species and three
     potentials, against the restatement.  In the mixed path the force passes carry their int64
     partial sums from one potential to the next."""

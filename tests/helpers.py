@@ -49,7 +49,7 @@ def workload(name: str) -> dict:
                     cm="linkedcell", cm_args="cutoff 8.5 nx 1 ny 1 nz 1",
                     pots=[("lennardjones", "sigma 3.405 epsilon 0.0103 cutoff 4.15", -1, -1)],
                     dt=1.0, nsteps=0, neigh=(1, 4.15))
-    if name == "lj_config1":
+    if name == "lj_ar_fcc10":
         pos, L = I.fcc_crystal3d(10, 10, 10, 5.26)
         m = np.full(len(pos), I.MASSES["Ar"])
         return dict(pos=pos, L=L, symbol="Ar", Z=18, vel=I.maxwell_boltzmann(m, 100.0, seed=1),
@@ -140,7 +140,7 @@ def workload(name: str) -> dict:
     raise KeyError(name)
 
 
-GOLDEN_CASES = ["kat108", "lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_fastlj", "lj_auto",
+GOLDEN_CASES = ["kat108", "lj_ar_fcc10", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au", "lj_fastlj", "lj_auto",
                 "lj_nx2", "lj_lcbinary", "lj_lcbinary_grow"]
 FP64_ONLY_CASES = {"lj_fastlj"}  # fastlj has no mixed-precision form
 # integrators other than velocityverlet (fixtures from the reference's own plugins)

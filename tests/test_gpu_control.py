@@ -1,5 +1,5 @@
 """The control file of the small Lennard-Jones argon case, run by the control-file runner on the
-GPU, against the reference's own run of the same system (golden fixture lj_config1: FCC 10^3,
+GPU, against the reference's own run of the same system (golden fixture lj_ar_fcc10: FCC 10^3,
 linkedcell nx 6, velocityverlet dt 1 fs, 100 steps, FP64)."""
 import numpy as np
 import pytest
@@ -50,8 +50,8 @@ integrator velocityverlet
 """
 
 
-def test_config1_control_file_matches_reference_run(tmp_path):
-    g = load_golden("lj_config1")
+def test_ar_fcc10_control_file_matches_reference_run(tmp_path):
+    g = load_golden("lj_ar_fcc10")
     L = g["L"]
     ctl = C.parse(control_text(float(L[0])), strict=True)
     out = C.run(ctl, precision="fp64", workdir=tmp_path)
@@ -132,7 +132,7 @@ def test_sutton_chen_control_file_with_thermostat_and_frames(precision, tmp_path
 def test_input_from_an_lpmd_file(tmp_path):
     from lpmd2_gb300 import formats as F
 
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     L = np.asarray(g["L"], float)
     w = F.LPMDWriter(tmp_path / "start.lpmd", level=1)
     w.write_header()
@@ -207,7 +207,7 @@ integrator beeman
 def test_dump_restore_continues_from_the_dumped_step(tmp_path):
     from lpmd2_gb300 import formats as F
 
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     L = float(np.asarray(g["L"])[0])
     base = control_text(L).replace("steps 100", "steps 20").replace("output xyz last.xyz each=100 level=1\n", "")
     base = base.replace("monitor step,potential-energy,kinetic-energy,temperature each=1 output=monitor.dat",

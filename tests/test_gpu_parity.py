@@ -126,7 +126,7 @@ def test_fp64_trajectory(case):
         np.testing.assert_allclose(log[:, col], g["thermo"][:, col], rtol=1e-9, atol=1e-12)
 
 
-@pytest.mark.parametrize("case", ["lj_config1", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au"])
+@pytest.mark.parametrize("case", ["lj_ar_fcc10", "lj_liquid_vl", "sc_cu", "fs_fe", "fsx_mo", "gupta_au"])
 def test_mixed_forces_and_neighbors(case):
     g = load_golden(case)
     sim = make_sim(g, precision="mixed")
@@ -136,7 +136,7 @@ def test_mixed_forces_and_neighbors(case):
     assert rms_err(acc, g["acc0"]) <= 1e-5 * force_scale(g)
     assert abs(th[1] - g["thermo0"][1]) <= 1e-6 * abs(g["thermo0"][1])
     # On a perfect lattice every pair of a shell has the same FP32 rounding, so the errors of
-    # the ~1e5 virial terms add up instead of averaging out (2e-5 measured on lj_config1);
+    # the ~1e5 virial terms add up instead of averaging out (2e-5 measured on lj_ar_fcc10);
     # at thermalised states the virial meets 1e-5 (test_forces_at_thermalised_state).
     assert abs(th[5] - g["thermo0"][5]) <= 1e-4 * abs(g["thermo0"][5])
     check_neighbors(sim, g)
@@ -144,7 +144,7 @@ def test_mixed_forces_and_neighbors(case):
 
 
 def test_mixed_trajectory_tracks_fp64():
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     sim = make_sim(g, precision="mixed")
     sim.update_forces()
     sim.do_steps(100)
@@ -182,7 +182,7 @@ def test_deterministic_reruns():
 def test_cell_sort_matches_reference_order():
     """LinkedCell binning (plugins/linkedcell.cc:244-266): the device cell index of every
     atom and the (cell, index) order equal the restatement's head/next traversal."""
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     sim = make_sim(g)
     cell, order = sim.cell_sort([6, 6, 6])
     L = g["L"]
@@ -195,7 +195,7 @@ def test_cell_sort_matches_reference_order():
 
 
 def test_fixed_flags_match_oracle():
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     n = len(g["pos_in"])
     flags = np.zeros(n, dtype=np.uint8)
     flags[::7] = gbmd.FLAG_FIXEDPOS
@@ -218,7 +218,7 @@ def test_species_filter_matches_oracle(precision):
     """Potential::AppliesTo (liblpmd/simulation/potential.cc:25-27) with two species and three
     potentials, against the restatement.  In the mixed path the force passes carry their int64
     partial sums from one potential to the next."""
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     n = len(g["pos_in"])
     Z = np.where(np.arange(n) % 3 == 0, 36, 18).astype(np.int32)
     mass = np.where(Z == 36, 83.798, 39.948)
@@ -263,8 +263,8 @@ def test_missing_components():
 def test_outside_box_atoms_are_wrapped_like_the_reference():
     """crystal3d leaves the last column of sites at x > L (plugins/crystal3d.cc:93-101);
     binning wraps them (plugins/linkedcell.cc:251-253) and the forces stay those of the
-    reference (the lj_config1 golden input has such atoms)."""
-    g = load_golden("lj_config1")
+    reference (the lj_ar_fcc10 golden input has such atoms)."""
+    g = load_golden("lj_ar_fcc10")
     assert (g["pos_in"][:, 0] > g["L"][0]).any()
     sim = make_sim(g)
     sim.update_forces()

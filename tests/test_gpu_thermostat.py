@@ -108,7 +108,7 @@ def test_set_temperature_skips_tagged_atoms_and_berendsen_does_not(precision):
 
 def test_rescaled_run_continues_as_a_fresh_run():
     # linked cells: the FP64 force sums depend on positions only, not on a list's history
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     a = make_sim(g, "fp64")
     a.update_forces()
     a.do_steps(10)
@@ -156,7 +156,7 @@ def test_batch_scales_one_system_or_all():
 
 
 def test_control_file_thermostat(tmp_path):
-    g = load_golden("lj_config1")
+    g = load_golden("lj_ar_fcc10")
     L = float(np.asarray(g["L"])[0])
     text = f"""
 cell cubic {L!r}

@@ -145,6 +145,6 @@ def test_linkedcell_stencil_quirks():
     n, side, ci = oracle.linkedcell_geometry(L, 8.5, 0, 0, 0, mode_auto=True)
     assert side == 2 and ci == 125 and n[0] % 2 == 0
     g = load_golden("lj_auto")
-    full = load_golden("lj_config1")
+    full = load_golden("lj_ar_fcc10")
     # auto mode drops pairs: fewer neighbours than the complete 27-cell stencil
     assert g["neigh_counts"].sum() < full["neigh_counts"].sum()

@@ -296,6 +296,93 @@ __global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_
 #ifndef GBMD_FORCE_MIN_BLOCKS
 #define GBMD_FORCE_MIN_BLOCKS 8
 #endif
+// List groups per ring iteration of the pair force pass (1 or 2; the EAM force pass uses 1: two
+// groups spill its registers).
+#ifndef GBMD_PAIR_RING_GROUPS
+#define GBMD_PAIR_RING_GROUPS 2
+#endif
+
+// Streams the list groups of the calling warp's 32 atoms (32 x 16 bytes, contiguous for a
+// fixed group index) through the warp's RING-stage shared-memory ring with bulk asynchronous
+// copies, calling body(group q, this lane's uint4 of that group) for q < ngw, the warp's
+// largest group count.  Lane 0 issues the copies; every wait is bounded.  Returns false if a
+// wait gave up.
+template <class F>
+__device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
+                                               uint4 (*ring)[32], unsigned long long* bar, F&& body) {
+  const int lane = threadIdx.x & 31;
+  const uint4* src0 = list_group(D, S, wfirst, 0);
+  const unsigned bytes = (unsigned)wcount * 16u;
+  const int na = S.natoms;
+  if (lane == 0 && ngw > 0) {
+    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
+    mbar_init_fence();
+    for (int r = 0; r < RING && r < ngw; ++r) {
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
+    }
+  }
+  __syncwarp();
+  bool waited = true;
+  for (int q = 0; q < ngw; ++q) {
+    const int r = q & (RING - 1);
+    if (!mbar_wait_bounded(&bar[r], (unsigned)((q / RING) & 1))) waited = false;
+    const uint4 cur = ring[r][lane];
+    __syncwarp();  // every lane has its entry: the stage can be refilled
+    if (lane == 0 && q + RING < ngw) {
+      fence_proxy_async_shared();
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)(q + RING) * na, bytes, &bar[r]);
+    }
+    body(q, cur);
+  }
+  return waited;
+}
+
+// As warp_list_ring, two groups per iteration: both stages are read before either body runs,
+// so the two groups' neighbour gathers can be in flight together (for latency-bound bodies).
+template <class F>
+__device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
+                                                uint4 (*ring)[32], unsigned long long* bar, F&& body) {
+  const int lane = threadIdx.x & 31;
+  const uint4* src0 = list_group(D, S, wfirst, 0);
+  const unsigned bytes = (unsigned)wcount * 16u;
+  const int na = S.natoms;
+  if (lane == 0 && ngw > 0) {
+    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
+    mbar_init_fence();
+    for (int r = 0; r < RING && r < ngw; ++r) {
+      mbar_expect_tx(&bar[r], bytes);
+      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
+    }
+  }
+  __syncwarp();
+  bool waited = true;
+  for (int q = 0; q < ngw; q += 2) {
+    const bool two = q + 1 < ngw;
+    const int r0 = q & (RING - 1), r1 = (q + 1) & (RING - 1);
+    if (!mbar_wait_bounded(&bar[r0], (unsigned)((q / RING) & 1))) waited = false;
+    if (two && !mbar_wait_bounded(&bar[r1], (unsigned)(((q + 1) / RING) & 1))) waited = false;
+    const uint4 c0 = ring[r0][lane];
+    const uint4 c1 = two ? ring[r1][lane] : make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();  // every lane has its entries: the stages can be refilled
+    if (lane == 0) {
+      fence_proxy_async_shared();
+      if (q + RING < ngw) {
+        mbar_expect_tx(&bar[r0], bytes);
+        bulk_g2s(ring[r0], src0 + (long long)(q + RING) * na, bytes, &bar[r0]);
+      }
+      if (two && q + 1 + RING < ngw) {
+        mbar_expect_tx(&bar[r1], bytes);
+        bulk_g2s(ring[r1], src0 + (long long)(q + 1 + RING) * na, bytes, &bar[r1]);
+      }
+    }
+    body(q, c0);
+    if (two) body(q + 1, c1);
+  }
+  return waited;
+}
+
 
 template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
 __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
@@ -325,7 +412,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
   __shared__ __align__(16) uint4 ring[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar[TILE / 32][RING];
   {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
     const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = __float_as_int(gi.w);
     const float phi_i = (PC == PC_EAM && active) ? D.phif[i] : 0.f;
@@ -377,29 +464,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
-    const uint4* src0 = list_group(D, S, wfirst, 0);
-    const unsigned bytes = (unsigned)wcount * 16u;
-    unsigned long long* wbar = bar[w];
-    if (lane == 0 && ngw > 0) {
-      for (int r = 0; r < RING; ++r) mbar_init(&wbar[r], 1);
-      mbar_init_fence();
-      for (int r = 0; r < RING && r < ngw; ++r) {
-        mbar_expect_tx(&wbar[r], bytes);
-        bulk_g2s(ring[w][r], src0 + (long long)r * na, bytes, &wbar[r]);
-      }
-    }
-    __syncwarp();
-    bool waited = true;
-    for (int q = 0; q < ngw; ++q) {
-      const int r = q & (RING - 1);
-      if (!mbar_wait_bounded(&wbar[r], (unsigned)((q / RING) & 1))) waited = false;
-      const uint4 cur = ring[w][r][lane];
-      __syncwarp();  // every lane has its entry: the stage can be refilled
-      if (lane == 0 && q + RING < ngw) {
-        fence_proxy_async_shared();
-        mbar_expect_tx(&wbar[r], bytes);
-        bulk_g2s(ring[w][r], src0 + (long long)(q + RING) * na, bytes, &wbar[r]);
-      }
+    auto group = [&](int q, const uint4& cur) {
       if (q < ng) {
         const int rem = cnt - 4 * q;
         float ax, ay, az, bx, by, bz;
@@ -417,7 +482,12 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
         // |group force| < 4096 eV/A keeps the fixed-point split exact
         bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
       }
-    }
+    };
+    bool waited;
+    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2)
+      waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], group);
+    else
+      waited = warp_list_ring(D, S, wfirst, wcount, ngw, ring[w], bar[w], group);
     if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
     if (band_e != NO_BAND) {
       // exact FP64 cutoff decision (the reference's Displacement and r^2) for the guard-band
@@ -704,87 +774,6 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
 // ------------------------------------------------------------------------------------------
 // EAM density pass + embedding (FP64 embedding in both precisions).
 // ------------------------------------------------------------------------------------------
-
-// Streams the list groups of the calling warp's 32 atoms (32 x 16 bytes, contiguous for a
-// fixed group index) through the warp's RING-stage shared-memory ring with bulk asynchronous
-// copies, calling body(group q, this lane's uint4 of that group) for q < ngw, the warp's
-// largest group count.  Lane 0 issues the copies; every wait is bounded.  Returns false if a
-// wait gave up.
-template <class F>
-__device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
-                                               uint4 (*ring)[32], unsigned long long* bar, F&& body) {
-  const int lane = threadIdx.x & 31;
-  const uint4* src0 = list_group(D, S, wfirst, 0);
-  const unsigned bytes = (unsigned)wcount * 16u;
-  const int na = S.natoms;
-  if (lane == 0 && ngw > 0) {
-    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
-    mbar_init_fence();
-    for (int r = 0; r < RING && r < ngw; ++r) {
-      mbar_expect_tx(&bar[r], bytes);
-      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
-    }
-  }
-  __syncwarp();
-  bool waited = true;
-  for (int q = 0; q < ngw; ++q) {
-    const int r = q & (RING - 1);
-    if (!mbar_wait_bounded(&bar[r], (unsigned)((q / RING) & 1))) waited = false;
-    const uint4 cur = ring[r][lane];
-    __syncwarp();  // every lane has its entry: the stage can be refilled
-    if (lane == 0 && q + RING < ngw) {
-      fence_proxy_async_shared();
-      mbar_expect_tx(&bar[r], bytes);
-      bulk_g2s(ring[r], src0 + (long long)(q + RING) * na, bytes, &bar[r]);
-    }
-    body(q, cur);
-  }
-  return waited;
-}
-
-// As warp_list_ring, two groups per iteration: both stages are read before either body runs,
-// so the two groups' neighbour gathers can be in flight together (for latency-bound bodies).
-template <class F>
-__device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
-                                                uint4 (*ring)[32], unsigned long long* bar, F&& body) {
-  const int lane = threadIdx.x & 31;
-  const uint4* src0 = list_group(D, S, wfirst, 0);
-  const unsigned bytes = (unsigned)wcount * 16u;
-  const int na = S.natoms;
-  if (lane == 0 && ngw > 0) {
-    for (int r = 0; r < RING; ++r) mbar_init(&bar[r], 1);
-    mbar_init_fence();
-    for (int r = 0; r < RING && r < ngw; ++r) {
-      mbar_expect_tx(&bar[r], bytes);
-      bulk_g2s(ring[r], src0 + (long long)r * na, bytes, &bar[r]);
-    }
-  }
-  __syncwarp();
-  bool waited = true;
-  for (int q = 0; q < ngw; q += 2) {
-    const bool two = q + 1 < ngw;
-    const int r0 = q & (RING - 1), r1 = (q + 1) & (RING - 1);
-    if (!mbar_wait_bounded(&bar[r0], (unsigned)((q / RING) & 1))) waited = false;
-    if (two && !mbar_wait_bounded(&bar[r1], (unsigned)(((q + 1) / RING) & 1))) waited = false;
-    const uint4 c0 = ring[r0][lane];
-    const uint4 c1 = two ? ring[r1][lane] : make_uint4(0u, 0u, 0u, 0u);
-    __syncwarp();  // every lane has its entries: the stages can be refilled
-    if (lane == 0) {
-      fence_proxy_async_shared();
-      if (q + RING < ngw) {
-        mbar_expect_tx(&bar[r0], bytes);
-        bulk_g2s(ring[r0], src0 + (long long)(q + RING) * na, bytes, &bar[r0]);
-      }
-      if (two && q + 1 + RING < ngw) {
-        mbar_expect_tx(&bar[r1], bytes);
-        bulk_g2s(ring[r1], src0 + (long long)(q + 1 + RING) * na, bytes, &bar[r1]);
-      }
-    }
-    body(q, c0);
-    if (two) body(q + 1, c1);
-  }
-  return waited;
-}
 
 // Mixed density pass over the Verlet list: FP32 rho_ij of each group of four entries
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point

@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_
 #ifndef GBMD_FORCE_MIN_BLOCKS
 #define GBMD_FORCE_MIN_BLOCKS 8
 #endif
+
 // List groups per ring iteration of the pair force pass (1 or 2; the EAM force pass uses 1: two
 // groups spill its registers).
 #ifndef GBMD_PAIR_RING_GROUPS
@@ -412,7 +413,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
   __shared__ __align__(16) uint4 ring[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar[TILE / 32][RING];
   {
-    const int w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = __float_as_int(gi.w);
     const float phi_i = (PC == PC_EAM && active) ? D.phif[i] : 0.f;
@@ -464,30 +465,71 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
-    auto group = [&](int q, const uint4& cur) {
-      if (q < ng) {
-        const int rem = cnt - 4 * q;
-        float ax, ay, az, bx, by, bz;
-        float g0 = pair(cur.x, true, ax, ay, az);
-        float g1 = pair(cur.y, rem > 1, bx, by, bz);
-        float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
-        g0 = pair(cur.z, rem > 2, ax, ay, az);
-        g1 = pair(cur.w, rem > 3, bx, by, bz);
-        gx = fmaf(g1, bx, fmaf(g0, ax, gx));
-        gy = fmaf(g1, by, fmaf(g0, ay, gy));
-        gz = fmaf(g1, bz, fmaf(g0, az, gz));
-        fqx.add_scaled32(gx);
-        fqy.add_scaled32(gy);
-        fqz.add_scaled32(gz);
-        // |group force| < 4096 eV/A keeps the fixed-point split exact
-        bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+    bool waited = true;
+    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) {
+      // two list groups per iteration: eight neighbour gathers in flight per lane
+      waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], [&](int q, const uint4& cur) {
+        if (q < ng) {
+          const int rem = cnt - 4 * q;
+          float ax, ay, az, bx, by, bz;
+          float g0 = pair(cur.x, true, ax, ay, az);
+          float g1 = pair(cur.y, rem > 1, bx, by, bz);
+          float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
+          g0 = pair(cur.z, rem > 2, ax, ay, az);
+          g1 = pair(cur.w, rem > 3, bx, by, bz);
+          gx = fmaf(g1, bx, fmaf(g0, ax, gx));
+          gy = fmaf(g1, by, fmaf(g0, ay, gy));
+          gz = fmaf(g1, bz, fmaf(g0, az, gz));
+          fqx.add_scaled32(gx);
+          fqy.add_scaled32(gy);
+          fqz.add_scaled32(gz);
+          // |group force| < 4096 eV/A keeps the fixed-point split exact
+          bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+        }
+      });
+    } else {
+      // one group per iteration, written out here: through the helper the EAM body spills more
+      const uint4* src0 = list_group(D, S, wfirst, 0);
+      const unsigned bytes = (unsigned)wcount * 16u;
+      unsigned long long* wbar = bar[w];
+      if (lane == 0 && ngw > 0) {
+        for (int r = 0; r < RING; ++r) mbar_init(&wbar[r], 1);
+        mbar_init_fence();
+        for (int r = 0; r < RING && r < ngw; ++r) {
+          mbar_expect_tx(&wbar[r], bytes);
+          bulk_g2s(ring[w][r], src0 + (long long)r * na, bytes, &wbar[r]);
+        }
       }
-    };
-    bool waited;
-    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2)
-      waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], group);
-    else
-      waited = warp_list_ring(D, S, wfirst, wcount, ngw, ring[w], bar[w], group);
+      __syncwarp();
+      for (int q = 0; q < ngw; ++q) {
+        const int r = q & (RING - 1);
+        if (!mbar_wait_bounded(&wbar[r], (unsigned)((q / RING) & 1))) waited = false;
+        const uint4 cur = ring[w][r][lane];
+        __syncwarp();  // every lane has its entry: the stage can be refilled
+        if (lane == 0 && q + RING < ngw) {
+          fence_proxy_async_shared();
+          mbar_expect_tx(&wbar[r], bytes);
+          bulk_g2s(ring[w][r], src0 + (long long)(q + RING) * na, bytes, &wbar[r]);
+        }
+        if (q < ng) {
+          const int rem = cnt - 4 * q;
+          float ax, ay, az, bx, by, bz;
+          float g0 = pair(cur.x, true, ax, ay, az);
+          float g1 = pair(cur.y, rem > 1, bx, by, bz);
+          float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
+          g0 = pair(cur.z, rem > 2, ax, ay, az);
+          g1 = pair(cur.w, rem > 3, bx, by, bz);
+          gx = fmaf(g1, bx, fmaf(g0, ax, gx));
+          gy = fmaf(g1, by, fmaf(g0, ay, gy));
+          gz = fmaf(g1, bz, fmaf(g0, az, gz));
+          fqx.add_scaled32(gx);
+          fqy.add_scaled32(gy);
+          fqz.add_scaled32(gz);
+          // |group force| < 4096 eV/A keeps the fixed-point split exact
+          bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+        }
+      }
+    }
     if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
     if (band_e != NO_BAND) {
       // exact FP64 cutoff decision (the reference's Displacement and r^2) for the guard-band

@@ -259,6 +259,8 @@ def main():
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=32, help="jobs of the served stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--serve-sweep", default="10,20,50,100,200,500",
+                    help="arrival rates (jobs/s) of the latency sweep, comma-separated ('' to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -369,6 +371,13 @@ def main():
     eam = eam_metal(local, args.eam_steps) if args.eam_steps > 0 else None
     batched = batched_ensemble(local, args.batch_steps, rank=rank, world=world, dist=dist) if args.batch_steps > 0 else None
     served = served_stream(local, args.serve_jobs, args.serve_rate, rank, world, dist) if args.serve_jobs > 0 else None
+    sweep = []
+    if args.serve_jobs > 0 and args.serve_sweep.strip():
+        for rate in (float(x) for x in args.serve_sweep.split(",")):
+            r = served if rate == args.serve_rate else served_stream(local, args.serve_jobs, rate, rank, world, dist)
+            sweep.append({"rate_jobs_per_s": rate, "p50_latency_s": r["p50_latency_s"],
+                          "p99_latency_s": r["p99_latency_s"], "atom_steps_per_s": r["atom_steps_per_s"],
+                          "wall_s": r["wall_s"], "completed": r["completed"]})
 
     if rank != 0:
         return
@@ -395,6 +404,7 @@ def main():
         "eam": eam,
         "batched": batched,
         "served": served,
+        "served_sweep": sweep or None,
         "list_rebuilds_timed": stats1["list_rebuilds"] - stats0["list_rebuilds"],
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

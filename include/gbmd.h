@@ -175,8 +175,9 @@ gbmd_status gbmd_sim_set_precision(gbmd_sim* sim, int precision);
  *   "time_kernels"     1: CUDA-event timing of every kernel class (graph_mode 0), see gbmd_stats
  *   "stream_priority"  1: the highest stream priority, 0: the lowest (default); replaces the
  *                      stream, so read gbmd_*_stream afterwards
- *   "lanes_per_atom"   mixed Lennard-Jones force pass: 1 (default), 2, 4 or 8 lanes share an
- *                      atom's neighbour list (same forces bit for bit; for small systems) */
+ *   "lanes_per_atom"   mixed Lennard-Jones force pass: 1 (default), 2, 4, 8, 16 or 32 lanes
+ *                      share an atom's neighbour list, i.e. 32 to 1 atoms per warp (same
+ *                      forces bit for bit; for small systems) */
 gbmd_status gbmd_sim_set_option(gbmd_sim* sim, const char* key, const char* value);
 
 /* CombinedPotential::UpdateForces (liblpmd/lpmd/combinedpotential.h:39-52): zeroes

@@ -3,7 +3,7 @@
 The Verlet skin trades list length (work per force evaluation) against rebuild frequency;
 the cell edge of the list build ((cutoff + skin) or half of it, with a 27- or 125-cell
 stencil) trades candidates per atom against lanes per cell; lanes per atom in the force pass
-(1, 2, 4 or 8, i.e. 32 to 4 atoms per warp) trade per-lane work against parallelism for
+(1, 2, 4, 8, 16 or 32, i.e. 32 to 1 atoms per warp) trade per-lane work against parallelism for
 batches too small to fill the GPU.  None of the optima can be read off the workload, so each
 choice is timed on a sample of the ensemble and the fastest wins: the skin x cell grid at one
 lane per atom, then the lane counts at the best grid point (the lane count does not change
@@ -15,7 +15,7 @@ from typing import Callable
 
 SKINS_SIGMA = (0.2, 0.3, 0.4)
 CELL_SCALES = (1, 2)
-LANES_PER_ATOM = (1, 2, 4, 8)
+LANES_PER_ATOM = (1, 2, 4, 8, 16, 32)
 
 
 def tune_batch(make: Callable[[dict], object], ms_per_step: Callable[[object], float],

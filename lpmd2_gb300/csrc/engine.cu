@@ -918,8 +918,12 @@ struct Engine::Impl {
             species ? k_force32_lanes<1, 2><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 2><<<g, TILE, 0, s>>>(D, P, sp);
           else if (lanes == 4)
             species ? k_force32_lanes<1, 4><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 4><<<g, TILE, 0, s>>>(D, P, sp);
-          else
+          else if (lanes == 8)
             species ? k_force32_lanes<1, 8><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 8><<<g, TILE, 0, s>>>(D, P, sp);
+          else if (lanes == 16)
+            species ? k_force32_lanes<1, 16><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 16><<<g, TILE, 0, s>>>(D, P, sp);
+          else
+            species ? k_force32_lanes<1, 32><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 32><<<g, TILE, 0, s>>>(D, P, sp);
         } else if (pair_kind(P.kind)) {
           if (species)
             k_force32<PC_PAIR, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
@@ -1562,9 +1566,10 @@ void Engine::set_option(const std::string& key, const std::string& value) {
     I.set_priority(v != 0.0 ? 1 : 0);
     return;
   }
-  if (key == "lanes_per_atom") {  // mixed LJ force pass: 1 (bulk-copy ring), 2, 4 or 8 lanes per atom
+  if (key == "lanes_per_atom") {  // mixed LJ force pass: 1 (bulk-copy ring), 2, 4, 8, 16 or 32 lanes per atom
     const int l = (int)v;
-    if (l != 1 && l != 2 && l != 4 && l != 8) throw Error(1, "lanes_per_atom must be 1, 2, 4 or 8");
+    if (l != 1 && l != 2 && l != 4 && l != 8 && l != 16 && l != 32)
+      throw Error(1, "lanes_per_atom must be 1, 2, 4, 8, 16 or 32");
     I.lanes = l;
     I.drop_graph();
     return;

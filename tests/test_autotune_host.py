@@ -19,8 +19,8 @@ def test_picks_fastest_and_closes_every_trial():
     assert best == {"skin_sigma": 0.3, "cell_scale": 1, "lanes_per_atom": 4}
     # the skin x cell grid at one lane, then the other lane counts at the best grid point
     assert len(trials) == len(SKINS_SIGMA) * len(CELL_SCALES) + len(LANES_PER_ATOM) - 1 == len(closed)
-    assert [t["lanes_per_atom"] for t in trials[-3:]] == [2, 4, 8]
-    assert all(t["skin_sigma"] == 0.3 and t["cell_scale"] == 1 for t in trials[-3:])
+    assert [t["lanes_per_atom"] for t in trials[-5:]] == [2, 4, 8, 16, 32]
+    assert all(t["skin_sigma"] == 0.3 and t["cell_scale"] == 1 for t in trials[-5:])
     assert all(s.closed for s in closed)
 
 

@@ -119,7 +119,7 @@ def test_inactive_system_is_frozen_and_others_run_on():
     b.close()
 
 
-@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
 def test_lanes_per_atom_give_the_same_trajectory(lanes):
     # the list groups of an atom are summed exactly as with one lane, and the lanes' fixed-point
     # partials combine exactly: forces and positions are bitwise those of one lane per atom;

@@ -248,7 +248,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gbmd", choices=["gbmd", "reference"])
-    ap.add_argument("--melt", type=int, default=1000, help="untimed mixed steps that melt the lattice")
+    ap.add_argument("--melt", type=int, default=2000,
+                    help="untimed FP64 steps that melt the lattice into the common start (--profile: mixed steps)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
                     help="short direct-launch run of the workload for ncu (no timing, no JSON)")
@@ -278,12 +279,17 @@ def main():
     torch.cuda.set_device(local)
     w = workload()
     N = w["natoms"]
-    sim = make_sim(w, "mixed", device=local)
-    sim.update_forces()
+    # the common start of every measurement: the jittered lattice melted by the plain FP64 path
+    w_melt = w
     if args.melt:
-        sim.do_steps(args.melt)
-    p_melt, v_melt, _ = sim.atoms()
-    w_melt = dict(w, pos=p_melt, vel=v_melt)
+        melt = make_sim(w, "fp64", device=local)
+        melt.update_forces()
+        melt.do_steps(args.melt)
+        p_melt, v_melt, _ = melt.atoms()
+        melt.close()
+        w_melt = dict(w, pos=p_melt, vel=v_melt)
+    sim = make_sim(w_melt, "mixed", device=local)
+    sim.update_forces()
     sim.do_steps(args.warmup)
     sim.synchronize()
 
@@ -392,7 +398,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": "lj_liquid_fcc40_256k", "natoms": N, "rho_star": RHO_STAR, "T_star": T_STAR,
                    "cutoff_sigma": 2.5, "skin_sigma": 0.3, "dt_fs": w["dt"], "precision": "mixed",
-                   "graph_block": GRAPH_BLOCK, "melt_steps": args.melt, "seed": 2,
+                   "graph_block": GRAPH_BLOCK, "melt_steps": args.melt, "melt_precision": "fp64", "seed": 2,
                    "rng": "SplitMix64 (lpmd2_gb300/inputs.py)",
                    "l2": "flushed (256 MB write) before every 10-step graph block, outside the timing",
                    "parallelism": f"replicas x{world}"},

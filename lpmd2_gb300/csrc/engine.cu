@@ -858,7 +858,7 @@ struct Engine::Impl {
     k_bin<<<nb, 256, 0, s>>>(D);
     k_scan<<<nsys, 1024, 0, s>>>(D);
     k_scatter<<<nb, 256, 0, s>>>(D);
-    k_cellsort<<<nblocks(D.total_cells, 4), 128, 0, s>>>(D);
+    k_cellsort<<<nblocks(D.total_cells, SORT_WARPS), 32 * SORT_WARPS, 0, s>>>(D);
     k_permute<<<nb, 256, 0, s>>>(D);
     k_copyback<<<nb, 256, 0, s>>>(D);
     launched(6);

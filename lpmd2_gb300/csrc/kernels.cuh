@@ -191,10 +191,17 @@ __global__ void k_scatter(Dev D) {
 
 // One warp per cell over the cells of every system (flat index g; cell_sys maps it back):
 // orders the cell's slots by original index, the order in which LinkedCell's head/next lists
-// visit them.  Up to 32 atoms: each lane ranks its atom by counting smaller tags across the
-// warp; larger cells fall back to an insertion sort by lane 0.
-__global__ void k_cellsort(Dev D) {
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// visit them.  Each atom's rank is the number of smaller tags in its cell: up to 32 atoms the
+// lanes compare through shuffles, up to SORT_STAGE atoms (dense cells of a liquid, coarse
+// LinkedCell grids) through a copy of the cell's tags in shared memory; larger cells fall back
+// to an insertion sort by lane 0.
+constexpr int SORT_WARPS = 4;    // cells per block
+constexpr int SORT_STAGE = 256;  // atoms per cell ranked in shared memory
+__global__ void __launch_bounds__(32 * SORT_WARPS) k_cellsort(Dev D) {
+  __shared__ int s_tag[SORT_WARPS][SORT_STAGE];
+  __shared__ int s_idx[SORT_WARPS][SORT_STAGE];
+  const int w = threadIdx.x >> 5;
+  const int g = blockIdx.x * SORT_WARPS + w;
   if (g >= D.total_cells) return;
   const int s = D.cell_sys[g];
   if (!D.sst[s].need_rebuild) return;
@@ -210,6 +217,23 @@ __global__ void k_cellsort(Dev D) {
     }
     __syncwarp();
     if (lane < n) D.perm[b + rank] = v;
+    return;
+  }
+  if (n <= SORT_STAGE) {
+    int* tg = s_tag[w];
+    int* ix = s_idx[w];
+    for (int k = lane; k < n; k += 32) {
+      const int v = D.perm[b + k];
+      ix[k] = v;
+      tg[k] = D.tag[v];
+    }
+    __syncwarp();  // every slot is read before any is rewritten
+    for (int k = lane; k < n; k += 32) {
+      const int t = tg[k];
+      int rank = 0;
+      for (int m = 0; m < n; ++m) rank += (tg[m] < t) ? 1 : 0;
+      D.perm[b + rank] = ix[k];
+    }
     return;
   }
   if (lane != 0) return;

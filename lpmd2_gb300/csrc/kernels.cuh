@@ -193,8 +193,8 @@ __global__ void k_scatter(Dev D) {
 // orders the cell's slots by original index, the order in which LinkedCell's head/next lists
 // visit them.  Each atom's rank is the number of smaller tags in its cell: up to 32 atoms the
 // lanes compare through shuffles, up to SORT_STAGE atoms (dense cells of a liquid, coarse
-// LinkedCell grids) through a copy of the cell's tags in shared memory; larger cells fall back
-// to an insertion sort by lane 0.
+// LinkedCell grids) through a copy of the cell's tags in shared memory, and beyond that through
+// global scratch (n^2/32 compares per lane).
 constexpr int SORT_WARPS = 4;    // cells per block
 constexpr int SORT_STAGE = 256;  // atoms per cell ranked in shared memory
 __global__ void __launch_bounds__(32 * SORT_WARPS) k_cellsort(Dev D) {
@@ -236,17 +236,20 @@ __global__ void __launch_bounds__(32 * SORT_WARPS) k_cellsort(Dev D) {
     }
     return;
   }
-  if (lane != 0) return;
-  for (int k = 1; k < n; ++k) {
-    int v = D.perm[b + k];
-    int tv = D.tag[v];
-    int q = k - 1;
-    while (q >= 0 && D.tag[D.perm[b + q]] > tv) {
-      D.perm[b + q + 1] = D.perm[b + q];
-      --q;
-    }
-    D.perm[b + q + 1] = v;
+  // larger cells: the same ranks through global scratch, the cell's own slots [b, b + n) of the
+  // permutation staging (free until k_permute fills it)
+  int* const tags = D.sint;
+  int* const sorted = D.sint + D.N;
+  for (int k = lane; k < n; k += 32) tags[b + k] = D.tag[D.perm[b + k]];
+  __syncwarp();
+  for (int k = lane; k < n; k += 32) {
+    const int t = tags[b + k];
+    int rank = 0;
+    for (int m = 0; m < n; ++m) rank += (tags[b + m] < t) ? 1 : 0;
+    sorted[b + rank] = D.perm[b + k];
   }
+  __syncwarp();
+  for (int k = lane; k < n; k += 32) D.perm[b + k] = sorted[b + k];
 }
 
 __global__ void k_permute(Dev D) {

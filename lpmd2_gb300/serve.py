@@ -250,10 +250,12 @@ def summarize(results: list[JobResult], wall_s: float) -> dict:
 def lanes_for(live_atoms: int) -> int:
     """Lanes per atom of the LJ force pass for a batch with this many live atoms: below about
     60k atoms one lane per atom leaves the GPU partly idle.  Thresholds from GB300 timings of
-    single LJ liquids at rc 2.5 sigma (ms/step with 1/2/4/8 lanes: 864 atoms 0.050/0.041/0.038/
-    0.037; 4,000: 0.055/0.046/0.042/0.042; 16,384: 0.050/0.041/0.042/0.049; 55,296:
-    0.058/0.056/0.067/0.091; 256,000: 0.145/0.165/0.206/0.322).  Forces are the same for every
-    choice, so changing it never changes a job's trajectory."""
+    single LJ liquids at rc 2.5 sigma (ms/step with 1/2/4/8/16 lanes: 864 atoms 0.046/0.040/
+    0.036/0.035/0.034; 4,000: 0.051/0.043/0.040/0.039/0.043; 16,384: 0.047/0.039/0.041/0.047/
+    0.062; 55,296: 0.055/0.055/0.065/0.089/0.141; 256,000: 0.140/0.163/0.203/0.319/0.566).
+    Forces are the same for every choice, so changing it never changes a job's trajectory."""
+    if live_atoms < 1_000:
+        return 16
     if live_atoms < 10_000:
         return 4
     if live_atoms < 60_000:

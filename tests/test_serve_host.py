@@ -158,4 +158,5 @@ def test_backend_failure_surfaces():
 def test_lanes_follow_the_live_atoms():
     from lpmd2_gb300.serve import lanes_for
 
-    assert [lanes_for(n) for n in (500, 9_999, 10_000, 59_999, 60_000, 3_000_000)] == [4, 4, 2, 2, 1, 1]
+    assert [lanes_for(n) for n in (500, 999, 1_000, 9_999, 10_000, 59_999, 60_000, 3_000_000)] == \
+        [16, 16, 4, 4, 2, 2, 1, 1]

@@ -32,6 +32,14 @@ sys.path.insert(0, str(ROOT))
 SIGMA, EPS, MASS = 3.405, 0.0103, 39.948
 RHO_STAR, T_STAR = 0.8442, 1.5
 GRAPH_BLOCK = 10
+# Bytes one mixed LJ step moves per atom: the Verlet-list entries it reads (about 88 x 4 B at
+# rc + skin = 2.8 sigma), the FP32 gather copy (16 B read, 16 B written), positions (24 B read,
+# 24 B written), velocities and accelerations (48 B read, 48 B written), the FP64 gather copy
+# (32 B written), mass/forcefactor/flags (17 B) and the displacement reference (16 B): ~590 B,
+# 151 MB at 256,000 atoms, larger than GB300's 129 MB L2.
+WORKING_SET_NOTE = ("not flushed: inputs larger than L2 -- a step streams ~590 B per atom (Verlet list ~350 B, "
+                    "FP64 state and gather copies), 151 MB at 256,000 atoms, against the 129 MB L2; value and "
+                    "e2e are timed alike")
 
 
 def workload(ncell: int = 40, seed: int = 2):
@@ -258,6 +266,8 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000, help="NVE steps of the drift comparison")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched ensemble (0: skip)")
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
+    ap.add_argument("--eam-drift-steps", type=int, default=5000,
+                    help="NVE steps of the Sutton-Chen drift comparison, both paths (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=32, help="jobs of the served stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, jobs/s")
     ap.add_argument("--serve-sweep", default="10,20,50,100,200,500",
@@ -293,19 +303,15 @@ def main():
     sim.do_steps(args.warmup)
     sim.synchronize()
 
-    stream = torch.cuda.ExternalStream(sim.stream, device=local)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-
     def timed_blocks(s, k_total):
-        """k_total steps in graph blocks; L2 flushed (256 MB write) before every block,
-        outside the timed events.  Returns summed device time in ms."""
+        """k_total steps in graph blocks, CUDA events on the simulation's stream around each
+        block.  No L2 flush: a step streams more than the 129 MB L2 holds (WORKING_SET_NOTE),
+        the same treatment as the end-to-end run.  Returns summed device time in ms."""
         st = torch.cuda.ExternalStream(s.stream, device=local)
         ms = 0.0
         done = 0
         while done < k_total:
             b = min(GRAPH_BLOCK, k_total - done)
-            with torch.cuda.stream(st):
-                flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
@@ -326,7 +332,6 @@ def main():
     stats1 = sim.stats()
     ms = allmax(dist, ms)
     value = N * args.steps * world / (ms * 1e-3)
-    th_log = sim.thermo_log()
 
     # plain FP64 GPU path on the same (melted) state
     sim64 = make_sim(w_melt, "fp64", device=local)
@@ -345,6 +350,7 @@ def main():
     a64 = sim64b.atoms()[2]
     frel = float(np.sqrt(np.sum((am - a64) ** 2) / np.sum(a64 ** 2)))
     e_m, e_64 = simm.thermo()["potential_energy"], sim64b.thermo()["potential_energy"]
+    w_m, w_64 = simm.thermo()["virial"], sim64b.thermo()["virial"]
     del simm, sim64b
 
     # kernel timing pass (direct launches, events around the force kernel on its stream)
@@ -366,15 +372,8 @@ def main():
     step_bytes_per_atom = 168.0
     step_achieved = step_bytes_per_atom * N * args.steps / (ms * 1e-3) / 1e9
 
-    # energy drift over the timed region (linear fit of the total energy)
-    drift = None
-    if len(th_log) > 2:
-        t_ps = th_log[:, 0] * w["dt"] * 1e-3
-        slope = np.polyfit(t_ps, th_log[:, 3], 1)[0]  # eV per ps
-        drift = float(slope * 1e3 / N)  # eV/atom/ns
-
     drift_cmp = measure_drift(w_melt, local, args.drift_steps) if args.drift_steps > 0 else None
-    eam = eam_metal(local, args.eam_steps) if args.eam_steps > 0 else None
+    eam = eam_metal(local, args.eam_steps, args.eam_drift_steps) if args.eam_steps > 0 else None
     batched = batched_ensemble(local, args.batch_steps, rank=rank, world=world, dist=dist) if args.batch_steps > 0 else None
     served = served_stream(local, args.serve_jobs, args.serve_rate, rank, world, dist) if args.serve_jobs > 0 else None
     sweep = []
@@ -400,36 +399,74 @@ def main():
                    "cutoff_sigma": 2.5, "skin_sigma": 0.3, "dt_fs": w["dt"], "precision": "mixed",
                    "graph_block": GRAPH_BLOCK, "melt_steps": args.melt, "melt_precision": "fp64", "seed": 2,
                    "rng": "SplitMix64 (lpmd2_gb300/inputs.py)",
-                   "l2": "flushed (256 MB write) before every 10-step graph block, outside the timing",
+                   "l2": WORKING_SET_NOTE,
                    "parallelism": f"replicas x{world}"},
         "ns_per_day": value / N / world * w["dt"] * 86400 * 1e-6,
-        "fp64_value": value64 * world, "fp64_ms_per_step": ms64 / k64, "speedup_vs_fp64": value / (value64 * world),
-        "force_rms_rel_err_vs_fp64": frel, "epot_rel_err_vs_fp64": abs(e_m - e_64) / abs(e_64),
-        "drift_ev_per_atom_per_ns": drift,
-        "drift": drift_cmp,
-        "eam": eam,
+        "gpu_launches": launches,
+        "list_rebuilds_timed": stats1["list_rebuilds"] - stats0["list_rebuilds"],
+        # details first; the driver keeps the end of the line, where the summary and the
+        # contract's objects sit
         "batched": batched,
         "served": served,
         "served_sweep": sweep or None,
-        "list_rebuilds_timed": stats1["list_rebuilds"] - stats0["list_rebuilds"],
-        "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "traffic": traffic,
-                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
-                                       "(profiles/k_force32_lj_liquid_256k.md); the Verlet list dominates it",
-                     "kernel": "k_force32<pair> (fused LJ force + velocity kick + drift)",
-                     "bytes_per_atom": force_bytes_per_atom, "launch_ms": kt["force_ms"],
-                     "peak_source": peak_kind},
+        "eam": eam,
+        "drift": drift_cmp,
+        "kernel_ms": kt,
         "step_roofline": {"achieved": step_achieved, "peak": peak, "unit": "GB/s", "frac": step_achieved / peak,
                           "bytes_per_atom_step": step_bytes_per_atom},
         "flop_roofline": flop_roofline(value / world, RHO_STAR, clk.summary()),
-        "kernel_ms": kt,
+        "fp64_value": value64 * world, "fp64_ms_per_step": ms64 / k64,
+        "force_rms_rel_err_vs_fp64": frel, "epot_rel_err_vs_fp64": abs(e_m - e_64) / abs(e_64),
+        "virial_rel_err_vs_fp64": abs(w_m - w_64) / abs(w_64),
+        "speedup_vs_fp64": value / (value64 * world),
+        "summary": summarize_line(value, value64 * world, e2e, frel, abs(e_m - e_64) / abs(e_64),
+                                  abs(w_m - w_64) / abs(w_64), drift_cmp, eam, batched, served),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "traffic_source": "not measured in this run: dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "of one ncu capture, read from profiles/k_force32_lj_liquid_256k.md; the "
+                                       "Verlet list dominates it",
+                     "kernel": "k_force32<pair> (fused LJ force + velocity kick + drift)",
+                     "bytes_per_atom": force_bytes_per_atom, "launch_ms": kt["force_ms"],
+                     "peak_source": peak_kind},
         "e2e": e2e,
         "clocks": clk.summary(),
     }
     if cpu:
         out["cpu_baseline"] = cpu
     print(json.dumps(out))
+
+
+def summarize_line(value, value64, e2e, frel, erel, wrel, drift, eam, batched, served) -> dict:
+    """The benchmark's headline figures in one short object: the mixed/FP64 ratio with its
+    errors for each workload, NVE drift, and the served stream's latency against the batched
+    engine's throughput."""
+    r = lambda x, d=4: None if x is None else float(f"{x:.{d}g}")  # noqa: E731
+    out = {"lj_mixed_over_fp64": r(value / value64), "lj_e2e_atom_steps_per_s": r(e2e["value"]),
+           "lj_errors_vs_fp64": {"force_rms": r(frel, 3), "epot": r(erel, 3), "virial": r(wrel, 3)}}
+    if drift:
+        out["lj_drift_ev_per_atom_per_ns"] = {"mixed": r(drift["mixed_ev_per_atom_per_ns"], 3),
+                                             "fp64": r(drift["fp64_ev_per_atom_per_ns"], 3), "ns": r(drift["ns"], 3)}
+    if eam:
+        out["eam_mixed_over_fp64"] = r(eam["speedup_vs_fp64"])
+        out["eam_atom_steps_per_s"] = r(eam["value"])
+        for key, tag in (("errors_20_fp64_steps", "eam_errors_20_steps"), ("errors_after_timed_run", "eam_errors_bench_state")):
+            e = eam[key]
+            out[tag] = {"force_rms": r(e["force_rms_rel_err_vs_fp64"], 3), "epot": r(e["epot_rel_err_vs_fp64"], 3),
+                        "virial_pressure": r(e["virial_pressure_rel_err_vs_fp64"], 3)}
+        if eam.get("drift"):
+            d = eam["drift"]
+            out["eam_drift_ev_per_atom_per_ns"] = {"mixed": r(d["mixed_ev_per_atom_per_ns"], 3),
+                                                  "fp64": r(d["fp64_ev_per_atom_per_ns"], 3), "ns": r(d["ns"], 3)}
+    if batched:
+        out["ensemble_mixed_over_fp64"] = r(batched["speedup_vs_fp64"])
+        out["ensemble_atom_steps_per_s"] = r(batched["value"])
+    if served:
+        out["served"] = {"p50_s": r(served["p50_latency_s"], 3), "p99_s": r(served["p99_latency_s"], 3),
+                         "atom_steps_per_s": r(served["atom_steps_per_s"]), "jobs": served["completed"]}
+        if batched:
+            out["served"]["fraction_of_batched"] = r(served["atom_steps_per_s"] / batched["value"], 3)
+    return out
 
 
 def run_profile(args):
@@ -526,30 +563,9 @@ def profiled_traffic(name: str):
     return None
 
 
-def measure_drift(w, device: int, steps: int, chunk: int = 1000) -> dict:
-    """NVE total-energy drift of the mixed and the FP64 path from the same melted state: slope
-    of a linear fit of the total energy over `steps` steps, in eV/atom/ns."""
-    N = w["natoms"]
-    out = {"steps": steps, "ns": steps * w["dt"] * 1e-6}
-    for prec in ("mixed", "fp64"):
-        s = make_sim(w, prec, device=device)
-        s.update_forces()
-        s.thermo_log()
-        logs = []
-        done = 0
-        while done < steps:
-            k = min(chunk, steps - done)
-            s.do_steps(k)
-            logs.append(s.thermo_log())
-            done += k
-        log = np.concatenate(logs)
-        t_ns = log[:, 0] * w["dt"] * 1e-6
-        slope = float(np.polyfit(t_ns, log[:, 3], 1)[0]) / N
-        out[f"{prec}_ev_per_atom_per_ns"] = slope
-        out[f"{prec}_etot_rms_fluct_ev_per_atom"] = float(np.std(log[:, 3])) / N
-        s.close()
-    out["mixed_minus_fp64_ev_per_atom_per_ns"] = out["mixed_ev_per_atom_per_ns"] - out["fp64_ev_per_atom_per_ns"]
-    return out
+def measure_drift(w, device: int, steps: int) -> dict:
+    """NVE drift of the LJ liquid in both paths from the same melted state (nve_drift)."""
+    return nve_drift(lambda prec: make_sim(w, prec, device=device), w["natoms"], w["dt"], steps)
 
 
 def lj_batch_plugins(skin_sigma: float):
@@ -697,11 +713,12 @@ def make_eam_sim(precision: str, device: int = 0, state: dict | None = None, nce
     return sim, w["natoms"]
 
 
-def eam_metal(device: int, steps: int, ncell: int = 50) -> dict:
+def eam_metal(device: int, steps: int, drift_steps: int = 5000, ncell: int = 50) -> dict:
     """Sutton-Chen copper: FCC 50^3 at a = 3.61 A with 1 % of the sites removed (495,000 atoms),
     300 K, linkedcell nx 25 (cell edge = cutoff = 7.22 A), velocityverlet dt 2 fs.  Mixed and
-    FP64 throughput, and the mixed path's force RMS, energy and virial-pressure errors against
-    FP64 at the same state."""
+    FP64 throughput; the mixed path's force RMS, energy and virial-pressure errors against FP64
+    at the same positions, 20 steps from the lattice and after the timed run; and the NVE drift
+    of both paths over `drift_steps` steps (5,000 x 2 fs = 10 ps) from the lattice."""
     from lpmd2_gb300 import inputs as I
 
     w = I.sc_cu_system(ncell, seed=3)
@@ -710,34 +727,72 @@ def eam_metal(device: int, steps: int, ncell: int = 50) -> dict:
     def make(prec, state):
         return make_eam_sim(prec, device, state, ncell)[0]
 
-    # time the mixed path from the lattice; its final (thermalised) state is where the
-    # errors are measured: on the perfect lattice the forces nearly cancel
+    def errors(state) -> dict:
+        sm, s64 = make("mixed", state), make("fp64", state)
+        sm.update_forces()
+        s64.update_forces()
+        am, a64 = sm.atoms()[2], s64.atoms()[2]
+        tm, t64 = sm.thermo(), s64.thermo()
+        sm.close()
+        s64.close()
+        return {"force_rms_rel_err_vs_fp64": float(np.sqrt(np.sum((am - a64) ** 2) / np.sum(a64 ** 2))),
+                "epot_rel_err_vs_fp64": abs(tm["potential_energy"] - t64["potential_energy"]) / abs(t64["potential_energy"]),
+                "virial_pressure_rel_err_vs_fp64": abs(tm["virial_pressure"] - t64["virial_pressure"])
+                / abs(t64["virial_pressure"]),
+                "epot_ev": t64["potential_energy"], "virial_pressure_mpa": t64["virial_pressure"]}
+
+    # the state 20 FP64 steps from the lattice (where the tests compare with the oracle)
+    s20 = make("fp64", w)
+    s20.update_forces()
+    s20.do_steps(20)
+    p20, v20, _ = s20.atoms()
+    s20.close()
+    err20 = errors(dict(w, pos=p20, vel=v20))
+    # time the mixed path from the lattice; its final (thermalised) state is the second point
+    # where the errors are measured (on the perfect lattice the forces nearly cancel)
     sm = make("mixed", w)
     ms = time_batch(sm, device, 20, steps)
     st = sm.stats()
     pos, vel, _ = sm.atoms()
     sm.close()
-    hot = dict(w, pos=pos, vel=vel)
-    sm, s64 = make("mixed", hot), make("fp64", hot)
-    sm.update_forces()
-    s64.update_forces()
-    am, a64 = sm.atoms()[2], s64.atoms()[2]
-    tm, t64 = sm.thermo(), s64.thermo()
-    frel = float(np.sqrt(np.sum((am - a64) ** 2) / np.sum(a64 ** 2)))
-    sm.close()
+    err_hot = errors(dict(w, pos=pos, vel=vel))
+    s64 = make("fp64", w)
     k64 = max(GRAPH_BLOCK, steps // 5 // GRAPH_BLOCK * GRAPH_BLOCK)
     ms64 = time_batch(s64, device, GRAPH_BLOCK, k64)
     s64.close()
     value, value64 = N * steps / (ms * 1e-3), N * k64 / (ms64 * 1e-3)
-    return {"workload": "sc_cu_fcc50_vac1pct", "seed": 3, "natoms": N, "steps": steps, "value": value, "unit": "atom-steps/s",
-            "ms_per_step": ms / steps, "ns_per_day": value / N * 2.0 * 86400 * 1e-6, "fp64_value": value64,
-            "speedup_vs_fp64": value / value64, "force_rms_rel_err_vs_fp64": frel,
-            "epot_rel_err_vs_fp64": abs(tm["potential_energy"] - t64["potential_energy"]) / abs(t64["potential_energy"]),
-            "virial_pressure_rel_err_vs_fp64": abs(tm["virial_pressure"] - t64["virial_pressure"])
-            / abs(t64["virial_pressure"]),
-            "epot_ev": t64["potential_energy"], "virial_pressure_mpa": t64["virial_pressure"],
-            "errors_at": f"the state after {20 + steps} mixed steps from the lattice",
-            "neighbor_mode": st["neighbor_mode"], "list_radius": st["list_radius"]}
+    out = {"workload": "sc_cu_fcc50_vac1pct", "seed": 3, "natoms": N, "steps": steps, "value": value,
+           "unit": "atom-steps/s", "ms_per_step": ms / steps, "ns_per_day": value / N * 2.0 * 86400 * 1e-6,
+           "fp64_value": value64, "speedup_vs_fp64": value / value64,
+           "errors_20_fp64_steps": err20, "errors_after_timed_run": dict(err_hot, at=f"after {20 + steps} mixed steps"),
+           "neighbor_mode": st["neighbor_mode"], "list_radius": st["list_radius"]}
+    if drift_steps > 0:
+        out["drift"] = nve_drift(lambda prec: make(prec, w), N, 2.0, drift_steps)
+    return out
+
+
+def nve_drift(make, natoms: int, dt_fs: float, steps: int, chunk: int = 1000) -> dict:
+    """NVE total-energy drift of the mixed and the FP64 path: slope of a linear fit of the
+    per-step total energy over `steps` steps, in eV/atom/ns, and the RMS fluctuation."""
+    out = {"steps": steps, "ns": steps * dt_fs * 1e-6}
+    for prec in ("mixed", "fp64"):
+        s = make(prec)
+        s.update_forces()
+        s.thermo_log()
+        logs = []
+        done = 0
+        while done < steps:
+            k = min(chunk, steps - done)
+            s.do_steps(k)
+            logs.append(s.thermo_log())
+            done += k
+        s.close()
+        log = np.concatenate(logs)
+        t_ns = log[:, 0] * dt_fs * 1e-6
+        out[f"{prec}_ev_per_atom_per_ns"] = float(np.polyfit(t_ns, log[:, 3], 1)[0]) / natoms
+        out[f"{prec}_etot_rms_fluct_ev_per_atom"] = float(np.std(log[:, 3])) / natoms
+    out["mixed_minus_fp64_ev_per_atom_per_ns"] = out["mixed_ev_per_atom_per_ns"] - out["fp64_ev_per_atom_per_ns"]
+    return out
 
 
 if __name__ == "__main__":

@@ -266,6 +266,10 @@ gbmd_status gbmd_batch_synchronize(gbmd_batch* batch);
 gbmd_status gbmd_batch_thermo(gbmd_batch* batch, int sys, gbmd_thermo* out);
 gbmd_status gbmd_batch_stats(gbmd_batch* batch, gbmd_stats* out);
 gbmd_status gbmd_batch_stream(gbmd_batch* batch, void** stream);
+/* gbmd_sim_neighbors for system sys of the batch (CellManager::BuildNeighborList,
+ * liblpmd/lpmd/cellmanager.h:25), indices local to the system. */
+gbmd_status gbmd_batch_neighbors(gbmd_batch* batch, int sys, int full, double rcut, int64_t* counts,
+                                 int64_t* idx, int64_t cap, int64_t* total);
 /* gbmd_sim_scale_velocities for system `sys` of a batch (-1: every active system). */
 gbmd_status gbmd_batch_scale_velocities(gbmd_batch* batch, int sys, int mode, double target, double dt_over_tau);
 /* gbmd_sim_checkpoint_* for a whole batch. */
@@ -313,8 +317,9 @@ gbmd_status gbmd_selftest_bounded_wait(int device, int64_t polls, int* gave_up);
  * library, overwritten by every call; the caller's output buffers need not start at zero.
  * The first call on a device (with that device current) looks the array up, which may load
  * the module: make that first call before anything that must not see module loading, such
- * as stream capture.  Calls that overlap in time on one device (other host threads, other
- * streams) share the array and race: serialise them. */
+ * as stream capture.  The address is kept for the life of the process, so do not call this
+ * entry point on a device after cudaDeviceReset on it.  Calls that overlap in time on one
+ * device (other host threads, other streams) share the array and race: serialise them. */
 gbmd_status gbmd_pair_forces_static(const gbmd_plugin* plugin, const double* pos, int n, const double* box,
                                     double* force, double* out, void* stream);
 

@@ -82,6 +82,7 @@ PotParams finalize_potential(int kind, const double* v, int s1, int s2) {
     P.cutoff = v[2];
     const double s = v[0], e = v[1];
     P.f[0] = (float)(s * s);
+    P.f[4] = (float)(s * s - (double)P.f[0]);  // low part of sigma^2 (double-float)
     P.f[1] = (float)(48.0 * e);
     P.f[2] = (float)(24.0 * e);
     P.f[3] = (float)(4.0 * e);
@@ -124,8 +125,8 @@ PotParams finalize_potential(int kind, const double* v, int s1, int s2) {
     P.f[8] = (float)d;
   }
   P.rc2 = P.cutoff * P.cutoff;
-  P.f[12] = (float)(P.rc2 * (1.0 - 8e-6));
-  P.f[13] = (float)(P.rc2 * (1.0 + 8e-6));
+  P.f[12] = band_lo(P.rc2);
+  P.f[13] = band_hi(P.rc2);
   return P;
 }
 
@@ -697,6 +698,11 @@ gbmd_status gbmd_batch_stats(gbmd_batch* batch, gbmd_stats* out) {
 gbmd_status gbmd_batch_stream(gbmd_batch* batch, void** stream) {
   if (!stream) return fail(GBMD_ERR_INVALID, "null argument");
   BATCH_GUARD(*stream = batch->eng->stream());
+}
+
+gbmd_status gbmd_batch_neighbors(gbmd_batch* batch, int sys, int full, double rcut, int64_t* counts, int64_t* idx,
+                                 int64_t cap, int64_t* total) {
+  BATCH_GUARD(batch->eng->neighbors(sys, full, rcut, counts, idx, cap, total));
 }
 
 }  // extern "C"

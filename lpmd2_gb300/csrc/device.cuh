@@ -69,6 +69,7 @@ struct SysDev {
   int lc_side;          // reference stencil side (NB_CELLS)
   double d[3];          // cell edge
   float df[3];
+  float dfc[3];         // (d - df) / df: relative rounding of the FP32 cell edge (shift correction)
   float rlist2f;        // (cutoff + skin)^2 with a conservative margin
   double thresh2;       // rebuild when a displacement^2 exceeds this
   long long nl_base;
@@ -134,6 +135,8 @@ struct Dev {
   // EAM
   double *rho, *phi;
   float* phif;
+  float4* g32e;      // mixed density pass output: g32's offsets with the FP32 embedding factor
+                     // 1/sqrt(rho) in w, gathered by the force pass of single-species systems
   // multi-potential accumulation
   long long* facc;   // 3*N fixed point
   double* dacc;      // 3*N FP64
@@ -345,6 +348,16 @@ struct Fix {
     hi += __float_as_int(t) - MAGIC_BITS;
     lo += __float_as_int(u) - MAGIC_BITS;
   }
+  // add(f * 2^26) for |f| < 2^18: the energies and virials of a list group, whose range then
+  // needs no check (a group beyond 2^18 eV implies forces far beyond the checked 4096 eV/A)
+  __device__ __forceinline__ void add_scaled26(float f) {
+    float t = fmaf(f, 16.0f, MAGIC);
+    float h = t - MAGIC;
+    float r = fmaf(-h, 0.0625f, f);
+    float u = fmaf(r, 67108864.0f, MAGIC);
+    hi += __float_as_int(t) - MAGIC_BITS;
+    lo += __float_as_int(u) - MAGIC_BITS;
+  }
   __device__ __forceinline__ long long value() const { return ((long long)hi << 22) + (long long)lo; }
 };
 
@@ -360,6 +373,51 @@ __device__ __forceinline__ float rcp_approx(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+}
+
+// The hardware approximations above may err with a consistent sign, and raised to the high
+// powers of the EAM functionals (r^-11, r^-8) a bias of 1e-7 becomes a systematic ~1e-6
+// relative error of every pair term.  In the virial, where pair repulsion and many-body
+// attraction cancel to a few percent, that showed up as a 1e-5 error.  One Newton step
+// (y' = y + y (1 - x y^2) / 2, resp. y' = y + y (1 - x y)) leaves only the rounding of the
+// step itself, which is unbiased.
+__device__ __forceinline__ float rsqrt_nr(float x) {
+  const float y = rsqrtf(x);
+  const float e = fmaf(-x * y, y, 1.0f);
+  return fmaf(0.5f * y, e, y);
+}
+__device__ __forceinline__ float rcp_nr(float x) {
+  const float y = rcp_approx(x);
+  return fmaf(y, fmaf(-x, y, 1.0f), y);
+}
+
+// FP32 displacement and squared distance of a Verlet-list entry: cell shift of the entry's
+// code plus the difference of the cell-relative offsets.  The force, density and neighbour
+// export kernels all decide cutoffs on this value, so their pair sets agree bit for bit.
+// The shift table holds k * (FP32 cell edge); the edge's rounding is the same for every pair
+// that crosses a cell boundary, i.e. a uniform strain of the box of up to 6e-8, which the
+// virial (stiff: pair repulsion and attraction cancel) amplifies.  With GBMD_SHIFT_CORR the
+// exact edge is restored by one FMA per axis: dx + sh * (d - df) / df.
+#ifndef GBMD_SHIFT_CORR
+#define GBMD_SHIFT_CORR 1
+#endif
+struct ShiftCorr {
+  float x, y, z;
+};
+__device__ __forceinline__ ShiftCorr shift_corr(const SysDev& S) {
+  return ShiftCorr{S.dfc[0], S.dfc[1], S.dfc[2]};
+}
+__device__ __forceinline__ float entry_r2(const float4& gi, const float4& gj, const float4& sh, const ShiftCorr& c,
+                                          float& dx, float& dy, float& dz) {
+  dx = (sh.x + gj.x) - gi.x;
+  dy = (sh.y + gj.y) - gi.y;
+  dz = (sh.z + gj.z) - gi.z;
+#if GBMD_SHIFT_CORR
+  dx = fmaf(sh.x, c.x, dx);
+  dy = fmaf(sh.y, c.y, dy);
+  dz = fmaf(sh.z, c.z, dz);
+#endif
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
 }  // namespace gbmd

@@ -183,10 +183,10 @@ __global__ void k_export(Dev D, int s, double rc2, float rc2_lo, float rc2_hi, i
   for_each_candidate<NB>(D, S, i, [&](long long j, unsigned code) {
     bool in;
     if (MIXED) {
-      const float4 gj = D.g32[j];
-      const float4 sh = shifts[code];
-      float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-      float r2 = dx * dx + dy * dy + dz * dz;
+      // the force and density kernels' own decision: entry_r2, inside below rc2_lo, the exact
+      // FP64 test in the guard band [rc2_lo, rc2_hi)
+      float dx, dy, dz;
+      const float r2 = entry_r2(gi, D.g32[j], shifts[code], shift_corr(S), dx, dy, dz);
       in = r2 < rc2_lo || (r2 < rc2_hi && exact_inside(D, S, i, j, rc2));
     } else {
       const double4_32a pj = D.g64[j];
@@ -335,6 +335,7 @@ struct Engine::Impl {
       for (int a = 0; a < 3; ++a) {
         S.d[a] = S.L[a] / (double)S.n[a];
         S.df[a] = (float)S.d[a];
+        S.dfc[a] = (float)((S.d[a] - (double)S.df[a]) / (double)S.df[a]);
         S.ninv[a] = (double)S.n[a] / S.L[a];
       }
       S.ncells = S.n[0] * S.n[1] * S.n[2];
@@ -762,6 +763,7 @@ struct Engine::Impl {
       for (int q = 0; q < 3; ++q) {
         S.d[q] = L[q] / (double)S.n[q];
         S.df[q] = (float)S.d[q];
+        S.dfc[q] = (float)((S.d[q] - (double)S.df[q]) / (double)S.df[q]);
       }
       S.ncells = S.n[0] * S.n[1] * S.n[2];
       for (int q = 0; q < 3; ++q) S.ninv[q] = (double)S.n[q] / L[q];
@@ -975,6 +977,12 @@ struct Engine::Impl {
                        "table bin): use precision fp64");
     if (!configured) configure();
     CK(cudaSetDevice(device));
+    if (!D.g32e && precision == PREC_MIXED)
+      for (const auto& P : pots)
+        if (!pair_kind(P.kind)) {
+          D.g32e = alloc<float4>((size_t)N);  // the mixed EAM density pass writes it
+          break;
+        }
     if (integ.kind != INT_VV && !D.ist) {
       // history of the integrators other than velocityverlet, moved with the atoms at re-sorts
       D.ist = alloc<double>((size_t)IST_K * N);
@@ -1661,7 +1669,7 @@ void Engine::neighbors(int sys, int full, double rcut, int64_t* counts, int64_t*
   int half = 0;
   if (!full) half = (I.cm.kind == CM_LINKEDCELL || I.cm.kind == CM_LCBINARY) ? 1 : 2;
   const double rc2 = rcut * rcut;
-  const float lo = (float)(rc2 * (1.0 - 8e-6)), hi = (float)(rc2 * (1.0 + 8e-6));
+  const float lo = band_lo(rc2), hi = band_hi(rc2);
   const bool mixed = I.precision == PREC_MIXED;
   long long *dc = nullptr, *doff = nullptr, *didx = nullptr;
   CK(dev_malloc(&dc, sizeof(long long) * std::max(n, 1)));

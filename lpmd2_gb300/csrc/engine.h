@@ -139,6 +139,12 @@ struct PluginSpec {
   std::string get(const std::string& key) const;
 };
 
+// Guard band of the mixed path's FP32 cutoff test: a pair with FP32 r^2 below band_lo(rc2) is
+// inside, at or above band_hi(rc2) outside, in between it is decided by the reference's exact
+// FP64 r^2.  The band is >= 5x the worst FP32 error of r^2 on cell-relative offsets.
+inline float band_lo(double rc2) { return (float)(rc2 * (1.0 - 8e-6)); }
+inline float band_hi(double rc2) { return (float)(rc2 * (1.0 + 8e-6)); }
+
 PluginSpec make_plugin(const std::string& name, const std::string& args);
 void potential_eval(const PotParams& p, int what, const double* args, double* out);
 // Runs the bounded-wait failure path once (a wait nothing completes); returns 1 if it gave up.

@@ -9,6 +9,7 @@ namespace gbmd {
 
 enum PotClass { PC_PAIR = 0, PC_EAM = 1 };
 
+
 // Visits the candidate neighbours j of atom i under neighbour mode NB (compile-time).
 template <int NB, class F>
 __device__ __forceinline__ void for_each_candidate(const Dev& D, const SysDev& S, long long i, F&& f) {
@@ -115,6 +116,17 @@ __device__ __forceinline__ float finish_atom(const Dev& D, const SysDev& S, long
   }
   if (sp.epi == EPI_KICK_DRIFT) return drift_atom<MIXED>(D, S, i, sp.dt, sp.half_dt2, vx, vy, vz, ax, ay, az);
   return 0.0f;
+}
+
+// Kinetic energy and momentum of the calling warp's atoms as int64 fixed point (2^-44 units):
+// FP64 warp sums in a fixed shuffle order, rounded once, on lane 0 (zeros elsewhere).  A warp
+// never spans two systems (tiles start at a system's first atom), so the sums are the same in a
+// batch and alone.
+__device__ __forceinline__ void warp_kinetic_fix(double ke, double px, double py, double pz, long long (&k4)[4]) {
+  const double s[4] = {warp_sum(ke), warp_sum(px), warp_sum(py), warp_sum(pz)};
+  const bool lead = (threadIdx.x & 31) == 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) k4[k] = lead ? __double2ll_rn(s[k] * FIX_KE) : 0ll;
 }
 
 // Writes the tile's FP64 partials (slots [lo, hi) of the 16) with overwrite or accumulate.
@@ -303,11 +315,21 @@ __global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_
 #define GBMD_PAIR_RING_GROUPS 2
 #endif
 
+// After a bounded wait gave up at group q no further copies are issued; lane 0 then waits (again
+// bounded) for the copies already in flight -- groups q .. q+RING-1 below ngw, one per stage --
+// so the warp never leaves while the copy engine still writes into its stages.
+__device__ __forceinline__ void ring_drain(unsigned long long* bar, int q, int ngw) {
+  if ((threadIdx.x & 31) == 0)
+    for (int g = q; g < q + RING && g < ngw; ++g) mbar_wait_bounded(&bar[g & (RING - 1)], (unsigned)((g / RING) & 1));
+  __syncwarp();
+}
+
 // Streams the list groups of the calling warp's 32 atoms (32 x 16 bytes, contiguous for a
 // fixed group index) through the warp's RING-stage shared-memory ring with bulk asynchronous
 // copies, calling body(group q, this lane's uint4 of that group) for q < ngw, the warp's
 // largest group count.  Lane 0 issues the copies; every wait is bounded.  Returns false if a
-// wait gave up.
+// wait gave up: the warp then stops (uniformly), drains its copies in flight and skips the
+// remaining groups.
 template <class F>
 __device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, int wfirst, int wcount, int ngw,
                                                uint4 (*ring)[32], unsigned long long* bar, F&& body) {
@@ -324,10 +346,12 @@ __device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, in
     }
   }
   __syncwarp();
-  bool waited = true;
   for (int q = 0; q < ngw; ++q) {
     const int r = q & (RING - 1);
-    if (!mbar_wait_bounded(&bar[r], (unsigned)((q / RING) & 1))) waited = false;
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&bar[r], (unsigned)((q / RING) & 1)))) {
+      ring_drain(bar, q, ngw);
+      return false;
+    }
     const uint4 cur = ring[r][lane];
     __syncwarp();  // every lane has its entry: the stage can be refilled
     if (lane == 0 && q + RING < ngw) {
@@ -337,7 +361,7 @@ __device__ __forceinline__ bool warp_list_ring(const Dev& D, const SysDev& S, in
     }
     body(q, cur);
   }
-  return waited;
+  return true;
 }
 
 // As warp_list_ring, two groups per iteration: both stages are read before either body runs,
@@ -358,12 +382,15 @@ __device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, i
     }
   }
   __syncwarp();
-  bool waited = true;
   for (int q = 0; q < ngw; q += 2) {
     const bool two = q + 1 < ngw;
     const int r0 = q & (RING - 1), r1 = (q + 1) & (RING - 1);
-    if (!mbar_wait_bounded(&bar[r0], (unsigned)((q / RING) & 1))) waited = false;
-    if (two && !mbar_wait_bounded(&bar[r1], (unsigned)(((q + 1) / RING) & 1))) waited = false;
+    bool ok = mbar_wait_bounded(&bar[r0], (unsigned)((q / RING) & 1));
+    if (two && ok) ok = mbar_wait_bounded(&bar[r1], (unsigned)(((q + 1) / RING) & 1));
+    if (!__all_sync(0xffffffffu, ok)) {
+      ring_drain(bar, q, ngw);
+      return false;
+    }
     const uint4 c0 = ring[r0][lane];
     const uint4 c1 = two ? ring[r1][lane] : make_uint4(0u, 0u, 0u, 0u);
     __syncwarp();  // every lane has its entries: the stages can be refilled
@@ -381,9 +408,8 @@ __device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, i
     body(q, c0);
     if (two) body(q + 1, c1);
   }
-  return waited;
+  return true;
 }
-
 
 template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
 __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
@@ -396,13 +422,21 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     return;
   }
   load_shifts(S, shifts);
+  const ShiftCorr corr = shift_corr(S);
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;  // index within the system
   const long long i = S.atom_base + li;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
   const float4* __restrict__ g32 = D.g32 + S.atom_base;
-  Fix fqx, fqy, fqz;
-  // sab = sum over pairs of f_a * r_b with f = g * r; stress_ab = -sab/2, virial = -trace/2
-  float ep = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  // EAM without a species filter gathers the density pass's copy, whose w holds the
+  // neighbour's embedding factor (one 16-byte gather per pair instead of 16 + 4 bytes)
+  constexpr bool PHI_IN_W = PC == PC_EAM && !SPECIES;
+  const float4* __restrict__ gsrc = PHI_IN_W ? D.g32e + S.atom_base : g32;
+  // force, energy and virial: each group of four list entries is summed in FP32 and the group
+  // sum rounded into int64 fixed point (forces 2^-32 eV/A; energy and virial 2^-26 eV, scaled
+  // to the system accumulators' 2^-32 by an exact integer shift); stress components are summed
+  // in FP32 per atom (sab = sum of f_a * r_b with f = g * r; stress_ab = -sab/2), rounded once
+  Fix fqx, fqy, fqz, fqe, fqv;
+  float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
   const float rc2_lo = P.f[12], rc2_hi = P.f[13];
   unsigned rechecks = 0;
   bool bad = false;
@@ -425,18 +459,15 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     constexpr unsigned NO_BAND = 0xffffffffu;
     unsigned band_e = NO_BAND;
     bool band_more = false;
+    float ge = 0.f, gv = 0.f;  // the current group's energy and sum of g r^2
     // Branch-free body: every candidate is evaluated and out-of-range pairs are masked to
     // zero, so lanes never diverge on the cutoff test (70% of Verlet-list entries are inside).
     // Returns g with f = g * d; the caller sums a group's four forces in FP32 and adds the
     // group sum to the int64 fixed-point accumulators.
     auto pair = [&](unsigned e, bool valid, float& dx, float& dy, float& dz) -> float {
       const int j = (int)(e & LOCAL_MASK);
-      const float4 gj = g32[j];
-      const float4 sh = shifts[e >> CODE_SHIFT];
-      dx = (sh.x + gj.x) - gi.x;
-      dy = (sh.y + gj.y) - gi.y;
-      dz = (sh.z + gj.z) - gi.z;
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float4 gj = gsrc[j];
+      const float r2 = entry_r2(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
       bool in = valid && r2 < rc2_lo;
       if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // guard band: decided in FP64 after the loop
         if (band_e == NO_BAND)
@@ -449,10 +480,11 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       if (PC == PC_PAIR) {
         lj_pair32(P, rcp_approx(r2), g, en);
       } else {
-        eam_pair32_t<SCN, SCM>(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
+        eam_pair32_t<SCN, SCM>(P, r2, phi_i, PHI_IN_W ? gj.w : D.phif[S.atom_base + j], g, en);
       }
       g = in ? g : 0.0f;
-      ep += in ? en : 0.0f;
+      ge += in ? en : 0.0f;
+      gv = fmaf(g, r2, gv);
       const float fx = g * dx, fy = g * dy, fz = g * dz;
       sxx = fmaf(fx, dx, sxx);
       sxy = fmaf(fx, dy, sxy);
@@ -462,6 +494,28 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       szz = fmaf(fz, dz, szz);
       return g;
     };
+    // One group of four entries (rem = entries left in the atom's list from this group on).
+    auto group = [&](const uint4& cur, int rem) {
+      ge = 0.f;
+      gv = 0.f;
+      float ax, ay, az, bx, by, bz;
+      float g0 = pair(cur.x, true, ax, ay, az);
+      float g1 = pair(cur.y, rem > 1, bx, by, bz);
+      float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
+      g0 = pair(cur.z, rem > 2, ax, ay, az);
+      g1 = pair(cur.w, rem > 3, bx, by, bz);
+      gx = fmaf(g1, bx, fmaf(g0, ax, gx));
+      gy = fmaf(g1, by, fmaf(g0, ay, gy));
+      gz = fmaf(g1, bz, fmaf(g0, az, gz));
+      fqx.add_scaled32(gx);
+      fqy.add_scaled32(gy);
+      fqz.add_scaled32(gz);
+      // halved: the full list counts each pair twice; virial = -sum g r^2 / 2
+      fqe.add_scaled26(0.5f * ge);
+      fqv.add_scaled26(-0.5f * gv);
+      // |group force| < 4096 eV/A keeps the force split exact
+      bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
+    };
     const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
@@ -469,23 +523,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) {
       // two list groups per iteration: eight neighbour gathers in flight per lane
       waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], [&](int q, const uint4& cur) {
-        if (q < ng) {
-          const int rem = cnt - 4 * q;
-          float ax, ay, az, bx, by, bz;
-          float g0 = pair(cur.x, true, ax, ay, az);
-          float g1 = pair(cur.y, rem > 1, bx, by, bz);
-          float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
-          g0 = pair(cur.z, rem > 2, ax, ay, az);
-          g1 = pair(cur.w, rem > 3, bx, by, bz);
-          gx = fmaf(g1, bx, fmaf(g0, ax, gx));
-          gy = fmaf(g1, by, fmaf(g0, ay, gy));
-          gz = fmaf(g1, bz, fmaf(g0, az, gz));
-          fqx.add_scaled32(gx);
-          fqy.add_scaled32(gy);
-          fqz.add_scaled32(gz);
-          // |group force| < 4096 eV/A keeps the fixed-point split exact
-          bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
-        }
+        if (q < ng) group(cur, cnt - 4 * q);
       });
     } else {
       // one group per iteration, written out here: through the helper the EAM body spills more
@@ -503,7 +541,11 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       __syncwarp();
       for (int q = 0; q < ngw; ++q) {
         const int r = q & (RING - 1);
-        if (!mbar_wait_bounded(&wbar[r], (unsigned)((q / RING) & 1))) waited = false;
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(&wbar[r], (unsigned)((q / RING) & 1)))) {
+          ring_drain(wbar, q, ngw);  // stop issuing, wait for the copies in flight, skip the rest
+          waited = false;
+          break;
+        }
         const uint4 cur = ring[w][r][lane];
         __syncwarp();  // every lane has its entry: the stage can be refilled
         if (lane == 0 && q + RING < ngw) {
@@ -511,23 +553,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
           mbar_expect_tx(&wbar[r], bytes);
           bulk_g2s(ring[w][r], src0 + (long long)(q + RING) * na, bytes, &wbar[r]);
         }
-        if (q < ng) {
-          const int rem = cnt - 4 * q;
-          float ax, ay, az, bx, by, bz;
-          float g0 = pair(cur.x, true, ax, ay, az);
-          float g1 = pair(cur.y, rem > 1, bx, by, bz);
-          float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
-          g0 = pair(cur.z, rem > 2, ax, ay, az);
-          g1 = pair(cur.w, rem > 3, bx, by, bz);
-          gx = fmaf(g1, bx, fmaf(g0, ax, gx));
-          gy = fmaf(g1, by, fmaf(g0, ay, gy));
-          gz = fmaf(g1, bz, fmaf(g0, az, gz));
-          fqx.add_scaled32(gx);
-          fqy.add_scaled32(gy);
-          fqz.add_scaled32(gz);
-          // |group force| < 4096 eV/A keeps the fixed-point split exact
-          bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
-        }
+        if (q < ng) group(cur, cnt - 4 * q);
       }
     }
     if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
@@ -537,9 +563,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       auto settle = [&](unsigned e) {
         const int j = (int)(e & LOCAL_MASK);
         const float4 gj = g32[j];
-        const float4 sh = shifts[e >> CODE_SHIFT];
-        const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        float dx, dy, dz;
+        const float r2 = entry_r2(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
         if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
         ++rechecks;
         if (!exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) return;
@@ -554,8 +579,9 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
         fqx.add_scaled32(fx);
         fqy.add_scaled32(fy);
         fqz.add_scaled32(fz);
+        fqe.add_scaled26(0.5f * en);
+        fqv.add_scaled26(-0.5f * (g * r2));
         bad |= fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) > 4000.0f;
-        ep += en;
         sxx = fmaf(fx, dx, sxx);
         sxy = fmaf(fx, dy, sxy);
         sxz = fmaf(fx, dz, sxz);
@@ -599,13 +625,12 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     if (bad) atomicOr(&D.sst[s].error, ERR_FIXED);
   }
   track_displacement_warp(D, s, d2);
-  // per-atom energy and stress (halved: full list) to int64 fixed point; exact block sums and
-  // one integer atomic per quantity into the system's accumulators
-  const float es = (float)(0.5 * FIX_E);
-  const float ms = -es;
-  long long v[11] = {fix64(ep * es), fix64((sxx + syy + szz) * ms), fix64(sxx * ms), fix64(sxy * ms),
-                     fix64(sxz * ms), fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms),
-                     fix64(syz * ms), fix64(szz * ms)};
+  // energy and virial already in fixed point; per-atom stress (halved: full list) rounded to
+  // int64 once; exact block sums and one integer atomic per quantity into the system's slots
+  const float ms = (float)(-0.5 * FIX_E);
+  long long v[11] = {fqe.value() * 64, fqv.value() * 64, fix64(sxx * ms), fix64(sxy * ms), fix64(sxz * ms),
+                     fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms), fix64(syz * ms),
+                     fix64(szz * ms)};
   long long tot[11];
   block_sum<long long, 11>(v, tot);
   if (threadIdx.x == 0) {
@@ -613,11 +638,10 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     for (int k = 0; k < 11; ++k) atomicAdd(acc + k, (unsigned long long)tot[k]);
   }
   if (sp.last) {
-    // kinetic energy: FP64 warp sums in a fixed order, rounded once per warp to int64 (2^-44
-    // units); momentum: rounded per atom.  Exact int64 sums from there on.
-    const double kw = warp_sum(ke);
-    long long k4[4] = {(threadIdx.x & 31) == 0 ? __double2ll_rn(kw * FIX_KE) : 0ll, __double2ll_rn(px * FIX_KE),
-                       __double2ll_rn(py * FIX_KE), __double2ll_rn(pz * FIX_KE)};
+    // kinetic energy and momentum: FP64 warp sums in a fixed order, rounded once per warp to
+    // int64 (2^-44 units); exact int64 sums from there on
+    long long k4[4];
+    warp_kinetic_fix(ke, px, py, pz, k4);
     long long kt[4];
     block_sum<long long, 4>(k4, kt);
     if (threadIdx.x == 0) {
@@ -650,14 +674,15 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
     return;
   }
   load_shifts(S, shifts);
+  const ShiftCorr corr = shift_corr(S);
   const int sub = threadIdx.x % LANES;
   const int slot = part * APB + (int)threadIdx.x / LANES;  // atom within the tile
   const int li = D.tile_first[tile] - (int)S.atom_base + slot;
   const long long i = S.atom_base + li;
   const bool active = slot < D.tile_count[tile];
   const float4* __restrict__ g32 = D.g32 + S.atom_base;
-  Fix fqx, fqy, fqz;
-  float ep = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  Fix fqx, fqy, fqz, fqe, fqv;
+  float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
   const float rc2_lo = P.f[12], rc2_hi = P.f[13];
   unsigned rechecks = 0;
   bool bad = false;
@@ -669,14 +694,11 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
   constexpr unsigned NO_BAND = 0xffffffffu;
   unsigned band_e = NO_BAND;
   bool band_more = false;
+  float ge = 0.f, gv = 0.f;
   auto pair = [&](unsigned e, bool valid, float& dx, float& dy, float& dz) -> float {
     const int j = (int)(e & LOCAL_MASK);
     const float4 gj = g32[j];
-    const float4 sh = shifts[e >> CODE_SHIFT];
-    dx = (sh.x + gj.x) - gi.x;
-    dy = (sh.y + gj.y) - gi.y;
-    dz = (sh.z + gj.z) - gi.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float r2 = entry_r2(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
     bool in = valid && r2 < rc2_lo;
     if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
       if (band_e == NO_BAND)
@@ -688,7 +710,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
     float g, en;
     lj_pair32(P, rcp_approx(r2), g, en);
     g = in ? g : 0.0f;
-    ep += in ? en : 0.0f;
+    ge += in ? en : 0.0f;
+    gv = fmaf(g, r2, gv);
     const float fx = g * dx, fy = g * dy, fz = g * dz;
     sxx = fmaf(fx, dx, sxx);
     sxy = fmaf(fx, dy, sxy);
@@ -702,6 +725,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
   for (int q = sub; q < ng; q += LANES) {
     const uint4 cur = __ldg(L + (long long)q * na);
     const int rem = cnt - 4 * q;
+    ge = 0.f;
+    gv = 0.f;
     float ax, ay, az, bx, by, bz;
     float g0 = pair(cur.x, true, ax, ay, az);
     float g1 = pair(cur.y, rem > 1, bx, by, bz);
@@ -714,15 +739,16 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
     fqx.add_scaled32(gx);
     fqy.add_scaled32(gy);
     fqz.add_scaled32(gz);
+    fqe.add_scaled26(0.5f * ge);
+    fqv.add_scaled26(-0.5f * gv);
     bad |= fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) > 4000.0f;
   }
   if (band_e != NO_BAND) {
     auto settle = [&](unsigned e) {
       const int j = (int)(e & LOCAL_MASK);
       const float4 gj = g32[j];
-      const float4 sh = shifts[e >> CODE_SHIFT];
-      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float dx, dy, dz;
+      const float r2 = entry_r2(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
       if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
       ++rechecks;
       if (!exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) return;
@@ -733,8 +759,9 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
       fqx.add_scaled32(fx);
       fqy.add_scaled32(fy);
       fqz.add_scaled32(fz);
+      fqe.add_scaled26(0.5f * en);
+      fqv.add_scaled26(-0.5f * (g * r2));
       bad |= fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) > 4000.0f;
-      ep += en;
       sxx = fmaf(fx, dx, sxx);
       sxy = fmaf(fx, dy, sxy);
       sxz = fmaf(fx, dz, sxz);
@@ -788,11 +815,12 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
     if (bad) atomicOr(&D.sst[s].error, ERR_FIXED);
   }
   track_displacement_warp(D, s, d2);
-  const float es = (float)(0.5 * FIX_E);
-  const float ms = -es;
-  long long v[11] = {fix64(ep * es), fix64((sxx + syy + szz) * ms), fix64(sxx * ms), fix64(sxy * ms),
-                     fix64(sxz * ms), fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms),
-                     fix64(syz * ms), fix64(szz * ms)};
+  // energy and virial: every lane's own fixed-point partial (exact integer block sums), so they
+  // do not depend on the lane count; stress rounded per lane
+  const float ms = (float)(-0.5 * FIX_E);
+  long long v[11] = {fqe.value() * 64, fqv.value() * 64, fix64(sxx * ms), fix64(sxy * ms), fix64(sxz * ms),
+                     fix64(sxy * ms), fix64(syy * ms), fix64(syz * ms), fix64(sxz * ms), fix64(syz * ms),
+                     fix64(szz * ms)};
   long long tot[11];
   block_sum<long long, 11>(v, tot);
   if (threadIdx.x == 0) {
@@ -800,9 +828,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
     for (int k = 0; k < 11; ++k) atomicAdd(acc + k, (unsigned long long)tot[k]);
   }
   if (sp.last) {
-    const double kw = warp_sum(ke);
-    long long k4[4] = {(threadIdx.x & 31) == 0 ? __double2ll_rn(kw * FIX_KE) : 0ll, __double2ll_rn(px * FIX_KE),
-                       __double2ll_rn(py * FIX_KE), __double2ll_rn(pz * FIX_KE)};
+    long long k4[4];
+    warp_kinetic_fix(ke, px, py, pz, k4);
     long long kt[4];
     block_sum<long long, 4>(k4, kt);
     if (threadIdx.x == 0) {
@@ -830,6 +857,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   const SysDev& S = D.sysd[s];
   if (!S.active) return;  // whole block: one tile belongs to one system
   load_shifts(S, shifts);
+  const ShiftCorr corr = shift_corr(S);
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;
   const long long i = S.atom_base + li;
   const bool active = (int)threadIdx.x < D.tile_count[tile];
@@ -846,10 +874,8 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   bool band_more = false;
   auto term = [&](unsigned e, bool valid) -> float {
     const int j = (int)(e & LOCAL_MASK);
-    const float4 gj = g32[j];
-    const float4 sh = shifts[e >> CODE_SHIFT];
-    const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float dx, dy, dz;
+    const float r2 = entry_r2(gi, g32[j], shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
     const bool in = valid && r2 < rc2_lo;
     if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
       if (band_e == NO_BAND)
@@ -877,10 +903,8 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
   if (band_e != NO_BAND) {
     auto settle = [&](unsigned e) {
       const int j = (int)(e & LOCAL_MASK);
-      const float4 gj = g32[j];
-      const float4 sh = shifts[e >> CODE_SHIFT];
-      const float dx = (sh.x + gj.x) - gi.x, dy = (sh.y + gj.y) - gi.y, dz = (sh.z + gj.z) - gi.z;
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float dx, dy, dz;
+      const float r2 = entry_r2(gi, g32[j], shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
       if (!(r2 >= rc2_lo && r2 < rc2_hi)) return;
       ++rechecks;
       if (exact_inside_cold(&D, &S, i, S.atom_base + j, P.rc2)) q.add(eam_rho32_t<SCM>(P, r2) * scale);
@@ -908,6 +932,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
     D.rho[i] = rho;
     D.phi[i] = phi;
     D.phif[i] = (float)phi;
+    D.g32e[i] = make_float4(gi.x, gi.y, gi.z, (float)phi);
   }
   // FP64 embedding energies summed exactly as int64 fixed point (2^-32 eV per atom)
   long long v[1] = {active ? __double2ll_rn(F * FIX_E) : 0ll};

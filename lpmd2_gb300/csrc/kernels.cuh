@@ -294,11 +294,14 @@ __device__ __forceinline__ float home_offset(double x, double xc, double L, doub
   return of;
 }
 
-// Gather copies of atom p at position (xx, yy, zz): the FP64 double4 and, for Verlet lists,
-// the FP32 offset from the home-cell centre (returned, for displacement tracking).
+// Gather copies of atom p at position (xx, yy, zz): the FP64 double4 (not by the mixed path's
+// fused drift, WRITE64 = 0: no mixed kernel reads it, and a change of precision re-sorts, which
+// rewrites it) and, for Verlet lists, the FP32 offset from the home-cell centre (returned, for
+// displacement tracking).
+template <int WRITE64 = 1>
 __device__ __forceinline__ float4 write_gather(const Dev& D, const SysDev& S, long long p, double xx, double yy,
                                                double zz, int t, double4_32a* g64, float4* g32) {
-  g64[p] = make_double4_32a(xx, yy, zz, (double)t);
+  if (WRITE64) g64[p] = make_double4_32a(xx, yy, zz, (double)t);
   float4 g = make_float4(0.f, 0.f, 0.f, __int_as_float(t));
   if (S.mode == NB_LIST) {
     const double* c = D.ccentre + 3 * (long long)D.home[p];
@@ -556,7 +559,7 @@ __device__ __forceinline__ float drift_atom(const Dev& D, const SysDev& S, long 
   D.xo[i] = nx;
   D.yo[i] = ny;
   D.zo[i] = nz;
-  float4 g = write_gather(D, S, i, nx, ny, nz, D.type[i], D.g64o, D.g32o);
+  float4 g = write_gather<!MIXED>(D, S, i, nx, ny, nz, D.type[i], D.g64o, D.g32o);
   return S.mode == NB_LIST ? displacement2(D, i, g) : 0.0f;
 }
 

@@ -173,25 +173,28 @@ __device__ __forceinline__ void eam_pair64(const PotParams& P, double r, double 
 
 // ------------------------------------------------------------------------------------------
 // FP32 (mixed path).  Constants in P.f:
-//   LJ: f[0]=sigma^2, f[1]=48 eps, f[2]=24 eps, f[3]=4 eps
+//   LJ: f[0]=sigma^2, f[1]=48 eps, f[2]=24 eps, f[3]=4 eps, f[4]=sigma^2 - f[0]
 //   SC: f[0]=e*an, f[1]=-n*e*an, f[2]=0.5*m*c*e*am, f[3]=am
 //   FS/FSX: f[0..4]=c0..c4, f[5]=A, f[6]=B, f[7]=c, f[8]=d
 //   Gupta: f[0]=A, f[1]=-p/r0, f[2]=-A p/r0, f[3]=B q/r0, f[4]=-2q/r0, f[5]=r0
 // ------------------------------------------------------------------------------------------
 
-// g with F_i = g * r_ij, and the pair energy e; inv = 1/r^2.
+// g with F_i = g * r_ij, and the pair energy e; inv = 1/r^2.  sigma^2 enters as the double-float
+// f[0] + f[4]: its FP32 rounding would scale (sigma/r)^12 and (sigma/r)^6 differently for every
+// pair alike, a bias the virial (where the two terms cancel) amplifies.  (The hardware reciprocal
+// showed no such bias: refining it by a Newton step changed no error measurably.)
 __device__ __forceinline__ void lj_pair32(const PotParams& P, float inv, float& g, float& e) {
-  float x = P.f[0] * inv;
+  float x = fmaf(P.f[0], inv, P.f[4] * inv);  // one rounding of (f[0] + f[4]) * inv
   float r6 = x * x * x;
   g = -inv * r6 * (P.f[1] * r6 - P.f[2]);
   e = r6 * (P.f[3] * r6 - P.f[3]);
 }
 
 __device__ __forceinline__ float eam_rho32(const PotParams& P, float r2) {
-  if (P.kind == POT_GUPTA) return expf(P.f[4] * (r2 * rsqrtf(r2) - P.f[5]));
+  if (P.kind == POT_GUPTA) return expf(P.f[4] * (r2 * rsqrt_nr(r2) - P.f[5]));
   if (P.kind == POT_SC) {
     if (P.int_m >= 0 && (P.int_m & 1) == 0) return P.f[3] * ipow_f(__frcp_rn(r2), P.int_m >> 1);
-    float ir = rsqrtf(r2);
+    float ir = rsqrt_nr(r2);
     return P.f[3] * ((P.int_m >= 0) ? ipow_f(ir, P.int_m) : __powf(ir, (float)P.p[3]));
   } else {
     float r = sqrtf(r2);
@@ -223,18 +226,18 @@ __device__ __forceinline__ float ipow_c(float x) {
 __device__ __forceinline__ void eam_pair32(const PotParams& P, float r2, float phi_i, float phi_j, float& s,
                                            float& e) {
   if (P.kind == POT_GUPTA) {
-    const float ir = rsqrtf(r2), dr = r2 * ir - P.f[5];
+    const float ir = rsqrt_nr(r2), dr = r2 * ir - P.f[5];
     const float ex = expf(P.f[1] * dr);
     e = P.f[0] * ex;
     s = (P.f[2] * ex + P.f[3] * (phi_i + phi_j) * expf(P.f[4] * dr)) * ir;
   } else if (P.kind == POT_SC) {
-    float ir = rsqrtf(r2);
+    float ir = rsqrt_nr(r2);
     float irn = (P.int_n >= 0) ? ipow_f(ir, P.int_n) : __powf(ir, (float)P.p[2]);
     float irm1 = (P.int_m >= 0) ? ipow_f(ir, P.int_m + 1) : __powf(ir, (float)P.p[3] + 1.0f);
     e = P.f[0] * irn;
     s = (P.f[1] * irn * ir + P.f[2] * (phi_i + phi_j) * irm1) * ir;
   } else {
-    float r = r2 * rsqrtf(r2);
+    float r = r2 * rsqrt_nr(r2);
     float ir = 1.0f / r;
     const float c0 = P.f[0], c1 = P.f[1], c2 = P.f[2], c3 = P.f[3], c4 = P.f[4];
     const float A = P.f[5], B = P.f[6], c = P.f[7], d = P.f[8];
@@ -270,9 +273,9 @@ template <int M>
 __device__ __forceinline__ float eam_rho32_t(const PotParams& P, float r2) {
   if constexpr (M > 0) {
     if constexpr (M % 2 == 0)
-      return P.f[3] * ipow_c<M / 2>(rcp_approx(r2));
+      return P.f[3] * ipow_c<M / 2>(rcp_nr(r2));
     else
-      return P.f[3] * ipow_c<M>(rsqrtf(r2));
+      return P.f[3] * ipow_c<M>(rsqrt_nr(r2));
   } else {
     return eam_rho32(P, r2);
   }
@@ -282,7 +285,7 @@ template <int N, int M>
 __device__ __forceinline__ void eam_pair32_t(const PotParams& P, float r2, float phi_i, float phi_j, float& s,
                                              float& e) {
   if constexpr (N > 0) {
-    const float ir = rsqrtf(r2);
+    const float ir = rsqrt_nr(r2);
     const float irm1 = ipow_c<M + 1>(ir);
     const float irn = ipow_c<N>(ir);
     e = P.f[0] * irn;

@@ -8,8 +8,10 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the array's device
 // address with cudaGetSymbolAddress, which may load the module; the address is cached per
-// device.  Calls from several host threads or streams share the one array per device and
-// therefore must not overlap in time on the same device.
+// device for the life of the process.  cudaDeviceReset unloads the module and invalidates the
+// cached address, so a process that resets a device must not call this entry point on that
+// device afterwards.  Calls from several host threads or streams share the one array per device
+// and therefore must not overlap in time on the same device.
 
 #include <cuda_runtime.h>
 
@@ -30,6 +32,8 @@ constexpr int ST_MAX_ATOMS = GBMD_STATIC_MAX_ATOMS;
 constexpr int ST_MAX_BLOCKS = (ST_MAX_ATOMS + ST_THREADS - 1) / ST_THREADS;
 constexpr int ST_PART = 11;  // pair energy, virial, stress (9)
 constexpr int ST_MAX_DEVICES = 64;
+// block_sum (device.cuh) reduces one value per thread of a TILE-thread block
+static_assert(ST_THREADS == TILE, "k_pair_forces_static launches TILE threads per block");
 
 // Per-block partial sums (128 blocks x 11 doubles = 11 KB).  Each call's force launch writes
 // the slots of every block it runs before the reduction launch reads them, so nothing in the

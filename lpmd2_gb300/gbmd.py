@@ -115,6 +115,8 @@ _SIGS = {
     "gbmd_batch_thermo": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(Thermo)]),
     "gbmd_batch_stats": (ctypes.c_int, [_VP, ctypes.POINTER(Stats)]),
     "gbmd_batch_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "gbmd_batch_neighbors": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_double, _I64, _I64,
+                                            ctypes.c_int64, _I64]),
     "gbmd_batch_set_active": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int]),
     "gbmd_sim_scale_velocities": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "gbmd_batch_scale_velocities": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -540,3 +542,15 @@ class Batch:
         p = _VP()
         _check(self.lib.gbmd_batch_stream(self.h, ctypes.byref(p)))
         return p.value or 0
+
+    def neighbors(self, sys: int, full: bool, rcut: float):
+        """Simulation.neighbors for system `sys` (indices local to the system)."""
+        n = int(self.natoms[sys])
+        counts = np.zeros(n, dtype=np.int64)
+        total = ctypes.c_int64(0)
+        _check(self.lib.gbmd_batch_neighbors(self.h, sys, int(full), float(rcut), _p(counts, _I64), None, 0,
+                                             ctypes.byref(total)))
+        idx = np.zeros(max(total.value, 1), dtype=np.int64)
+        _check(self.lib.gbmd_batch_neighbors(self.h, sys, int(full), float(rcut), _p(counts, _I64), _p(idx, _I64),
+                                             total.value, ctypes.byref(total)))
+        return counts, idx[: total.value]

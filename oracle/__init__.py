@@ -38,14 +38,24 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I64 = ctypes.POINTER(ctypes.c_int64)
 
 
+def reference_source() -> Path | None:
+    """The lpmd2 checkout to compile the reference from: $LPMD_REFERENCE, else the checkout the
+    last `make ref` was built from (recorded in _ref/REFERENCE); None when neither names an
+    existing checkout."""
+    env = os.environ.get("LPMD_REFERENCE")
+    rec = HERE / "_ref" / "REFERENCE"
+    cand = Path(env) if env else (Path(rec.read_text().strip()) if rec.exists() else None)
+    return cand if cand is not None and (cand / "liblpmd").is_dir() else None
+
+
 def build(quiet: bool = True) -> None:
-    """Compiles liblpmd oracle (and the reference driver when the sources are present)."""
+    """Compiles the oracle (and the reference driver when reference_source() names a checkout)."""
     import subprocess
 
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", str(HERE), "liboracle.so"], check=True, stdout=out)
-    ref = os.environ.get("LPMD_REFERENCE", "/root/reference")
-    if Path(ref, "liblpmd").is_dir():
+    ref = reference_source()
+    if ref is not None:
         subprocess.run(["make", "-C", str(HERE), "-j8", "ref", f"REF={ref}"], check=True, stdout=out)
 
 

@@ -12,8 +12,10 @@ from pathlib import Path
 
 import pytest
 
+import oracle
+
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("LPMD_REFERENCE", "/root/reference"))
+REF = oracle.reference_source()  # $LPMD_REFERENCE or the checkout the reference build used
 REF_LIB = ROOT / "oracle" / "_ref" / "libref_driver.so"
 GBMD_LIB = ROOT / "lpmd2_gb300" / "libgbmd.so"
 
@@ -48,8 +50,8 @@ int main(int argc, char** argv) {
 
 @pytest.fixture(scope="module")
 def plugin(tmp_path_factory):
-    if not (REF / "liblpmd" / "lpmd" / "plugin.h").exists():
-        pytest.skip("no lpmd2 reference checkout here")
+    if REF is None or not (REF / "liblpmd" / "lpmd" / "plugin.h").exists():
+        pytest.skip("no lpmd2 reference checkout named (set LPMD_REFERENCE)")
     if not REF_LIB.exists() or not GBMD_LIB.exists():
         pytest.skip("reference build or libgbmd.so not built (run __graft_entry__.build())")
     subprocess.run(["make", "-s", "-C", str(ROOT / "lpmd2_gb300" / "lpmd_plugin"), f"LPMD={REF}"], check=True)

@@ -1,10 +1,18 @@
-"""gbmd_pair_forces_static (pair forces without device allocation) against the simulation path.
+"""gbmd_pair_forces_static: pair forces for callers that cannot allocate device memory.
 
-Both go through the C ABI.  The simulation path (gbmd_sim_* with the minimumimage cell
-manager, FP64) is the existing entry point; the static entry point must agree with it to
-1e-12 relative on forces, pair energy, virial and stress, on two calls in a row with
-different positions (the second call must not see anything the first one left behind).
-The file sorts last so that it also runs after every other GPU test in one session.
+Some callers cannot call cudaMalloc at the point where they need forces: a host program that
+hands its whole device memory budget to its own pool allocator up front, or a latency-bound
+loop that cannot afford an allocation's implicit synchronisation.  The static entry point
+takes positions, forces and sums in buffers the caller owns and keeps its only scratch in a
+fixed array inside the library.
+
+Checked through the C ABI, on two calls in a row, against (1) the existing simulation entry
+point (gbmd_sim_* with the minimumimage cell manager, FP64) to 1e-12 relative, and (2) the
+oracle's restatement of the reference's minimum-image pair forces on the same positions, to
+1e-12 relative.  The second call of each pair must not see anything the first one left in the
+shared scratch array: the calls differ in positions and, in the second test, in size (16,384
+atoms, the array's capacity, then 864).  The file sorts last so that it also runs after every
+other GPU test in one session; it needs nothing from them and passes alone in a fresh process.
 """
 import re
 from pathlib import Path
@@ -19,13 +27,15 @@ pytestmark = pytest.mark.gpu
 
 gbmd = pytest.importorskip("lpmd2_gb300.gbmd")
 torch = pytest.importorskip("torch")
+oracle = pytest.importorskip("oracle")
 
 FORCEFACTOR = 0.00964853  # eV/A/amu -> A/fs^2, the session's "forcefactor"
+TOL = 1e-12
 
 
 @pytest.fixture(scope="module", autouse=True)
 def _built():
-    if not gbmd.LIB_PATH.exists():
+    if not gbmd.LIB_PATH.exists() or not oracle.PORT_LIB.exists():
         import __graft_entry__
 
         __graft_entry__.build()
@@ -33,9 +43,10 @@ def _built():
         pytest.fail("no CUDA device: the GPU tests need a GB300")
 
 
-def _system(seed):
+def _system(k, seed):
+    """FCC k^3 argon at liquid density, jittered by up to 0.35 A (4k^3 atoms)."""
     a = (4.0 / 0.8442) ** (1.0 / 3.0) * 3.405
-    pos, L = I.fcc_fast(6, 6, 6, a)
+    pos, L = I.fcc_fast(k, k, k, a)
     pos = np.mod(I.jitter(pos, 0.35, seed=seed), L)
     return pos, L
 
@@ -58,37 +69,66 @@ def _simulation_path(pos, L, pot):
     return force, th["potential_energy"], th["virial"], th["stress"].ravel()
 
 
+def _oracle_path(pos, L):
+    """The same quantities from the oracle's minimum-image restatement of the reference."""
+    n = len(pos)
+    mass = np.full(n, I.MASSES["Ar"])
+    ref = oracle.run_port(pos, L, np.full(n, 18), mass, np.zeros_like(pos), "minimumimage", "cutoff 8.5",
+                          [("lennardjones", LJ_AR, -1, -1)], 1.0, 0)
+    th = ref["thermo0"]
+    force = ref["acc0"] / (FORCEFACTOR / mass)[:, None]
+    return force, th[1], th[5], th[13:22]
+
+
 def _static_path(pos, L, pot, force_d, out_d, stream):
-    pos_d = torch.from_numpy(np.ascontiguousarray(pos)).to("cuda")
-    force_d.fill_(float("nan"))  # every entry must be written by the call
+    n = len(pos)
+    pos_d = torch.from_numpy(np.ascontiguousarray(pos).ravel()).to("cuda")
+    force_d[: 3 * n].fill_(float("nan"))  # every entry the call owns must be written by it
     out_d.fill_(float("nan"))
-    gbmd.pair_forces_static(pot, pos_d.data_ptr(), len(pos), L, force_d.data_ptr(), out_d.data_ptr(),
-                            stream.cuda_stream)
+    # the upload and the fills above were queued on torch's current stream; the library's
+    # kernels go to `stream`, which must not start before them
+    stream.wait_stream(torch.cuda.current_stream())
+    gbmd.pair_forces_static(pot, pos_d.data_ptr(), n, L, force_d.data_ptr(), out_d.data_ptr(), stream.cuda_stream)
     stream.synchronize()
-    return force_d.cpu().numpy().reshape(-1, 3).copy(), out_d.cpu().numpy().copy()
+    return force_d[: 3 * n].cpu().numpy().reshape(-1, 3).copy(), out_d.cpu().numpy().copy()
 
 
-def test_static_matches_simulation_on_two_calls():
-    pot = gbmd.Plugin("lennardjones", LJ_AR)
-    stream = torch.cuda.Stream()
-    n = 864
-    force_d = torch.empty(3 * n, dtype=torch.float64, device="cuda")
-    out_d = torch.empty(11, dtype=torch.float64, device="cuda")
-    for seed in (11, 12):
-        pos, L = _system(seed)
-        assert len(pos) == n
-        f_ref, e_ref, w_ref, s_ref = _simulation_path(pos, L, pot)
-        f, out = _static_path(pos, L, pot, force_d, out_d, stream)
-        assert np.all(np.isfinite(f)) and np.all(np.isfinite(out))
-        assert rel_norm_err(f, f_ref) <= 1e-12
-        assert abs(out[0] - e_ref) <= 1e-12 * abs(e_ref)
-        assert abs(out[1] - w_ref) <= 1e-12 * abs(w_ref)
-        assert np.max(np.abs(out[2:] - s_ref)) <= 1e-12 * np.max(np.abs(s_ref))
+def _check(f, out, expect):
+    f_ref, e_ref, w_ref, s_ref = expect
+    assert np.all(np.isfinite(f)) and np.all(np.isfinite(out))
+    assert rel_norm_err(f, f_ref) <= TOL
+    assert abs(out[0] - e_ref) <= TOL * abs(e_ref)
+    assert abs(out[1] - w_ref) <= TOL * abs(w_ref)
+    assert np.max(np.abs(out[2:] - s_ref)) <= TOL * np.max(np.abs(s_ref))
 
 
 def _static_max() -> int:
     text = (Path(__file__).resolve().parents[1] / "include" / "gbmd.h").read_text()
     return int(re.search(r"#define GBMD_STATIC_MAX_ATOMS (\d+)", text).group(1))
+
+
+def _run_calls(cases):
+    pot = gbmd.Plugin("lennardjones", LJ_AR)
+    stream = torch.cuda.Stream()
+    nmax = max(4 * k ** 3 for k, _ in cases)
+    force_d = torch.empty(3 * nmax, dtype=torch.float64, device="cuda")
+    out_d = torch.empty(11, dtype=torch.float64, device="cuda")
+    for k, seed in cases:
+        pos, L = _system(k, seed)
+        f, out = _static_path(pos, L, pot, force_d, out_d, stream)
+        _check(f, out, _simulation_path(pos, L, pot))
+        _check(f, out, _oracle_path(pos, L))
+
+
+def test_static_matches_simulation_and_oracle_on_two_calls():
+    _run_calls([(6, 11), (6, 12)])  # 864 atoms, two different configurations
+
+
+def test_static_at_capacity_then_small():
+    # 16^3 FCC = 16,384 atoms fills the scratch array (128 blocks); the 864-atom call after it
+    # reduces over 7 blocks and must not pick up the larger call's partial sums
+    assert 4 * 16 ** 3 == _static_max()
+    _run_calls([(16, 13), (6, 14)])
 
 
 def test_static_rejects_sizes_beyond_its_scratch():

@@ -135,6 +135,10 @@ gbmd_status gbmd_plugin_cutoff(const gbmd_plugin* plugin, double* cutoff);
  *   what 2: rhoij(r)  (metal)                     args {r}                 out {rho}
  *   what 3: F(rho)    (metal)                     args {rho}               out {F}
  *   what 4: ManyBodies(r^, rhoi, rhoj, r) (metal) args {rx,ry,rz,rhoi,rhoj} out {Fx,Fy,Fz}
+ *   what 5: PairForce(normrij, rmod)  (metal)     args {nx,ny,nz,rmod}     out {Fx,Fy,Fz}
+ *   what 6: ManyBodies(normrij, rhoi, rhoj, rmod) args {nx,ny,nz,rhoi,rhoj,rmod} out {Fx,Fy,Fz}
+ *           (5 and 6 take the unit vector and modulus as the reference's virtuals receive them,
+ *           so their results are the reference's bit for bit)
  * PairPotential (liblpmd/lpmd/pairpotential.h:23-25), MetalPotential
  * (liblpmd/lpmd/metalpotential.h:26-35). */
 gbmd_status gbmd_potential_eval(const gbmd_plugin* plugin, int what, const double* args, double* out);

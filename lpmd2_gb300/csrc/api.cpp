@@ -321,11 +321,14 @@ void potential_eval(const PotParams& P, int what, const double* a, double* out) 
   } else if (what == 3) {
     double A = P.kind == POT_SC ? v[4] * v[0] : (P.kind == POT_FS || P.kind == POT_GUPTA) ? v[3] : v[5];
     out[0] = P.kind == POT_SC ? -v[4] * v[0] * std::sqrt(a[0]) : -A * std::sqrt(a[0]);
-  } else if (what == 1 || what == 4) {
-    double r = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-    double nrm[3] = {a[0] / r, a[1] / r, a[2] / r};
+  } else if (what == 1 || what == 4 || what == 5 || what == 6) {
+    // 1, 4: from r_ij; 5, 6: from the unit vector and the modulus as the reference's
+    // PairForce(normrij, rmod) / ManyBodies(normrij, rhoi, rhoj, rmod) receive them
+    const bool given = what >= 5;
+    double r = given ? a[what == 5 ? 3 : 5] : std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    double nrm[3] = {given ? a[0] : a[0] / r, given ? a[1] : a[1] / r, given ? a[2] : a[2] / r};
     double s = 0.0;
-    if (what == 1) {
+    if (what == 1 || what == 5) {
       if (P.kind == POT_GUPTA) {  // gupta.cc:60-62
         s = -(v[0] * v[2] / v[1]) * std::exp(-v[2] * (r - v[1]) / v[1]);
       } else if (P.kind == POT_SC) {

@@ -844,7 +844,8 @@ struct Engine::Impl {
   // --------------------------------------------------------------------------------------
 
   void launch_decide(cudaStream_t s, int ucall_inc, int force_all, cudaGraphConditionalHandle h, int use_cond) {
-    k_decide<<<1, 256, 0, s>>>(D, nsys, ucall_inc, force_all, (unsigned long long)h, use_cond);
+    k_decide<<<nblocks(nsys, DECIDE_THREADS), DECIDE_THREADS, 0, s>>>(D, nsys, ucall_inc, force_all,
+                                                                      (unsigned long long)h, use_cond);
     launched();
   }
 
@@ -964,7 +965,8 @@ struct Engine::Impl {
     }
     mark_end(s, T_FORCE);
     if (mixed)
-      k_tail<<<1, 256, 0, s>>>(D, count_step, decide_next, (unsigned long long)cond_next);
+      k_tail<<<nblocks(nsys, TAIL_THREADS), TAIL_THREADS, 0, s>>>(D, count_step, decide_next,
+                                                                  (unsigned long long)cond_next);
     else
       k_thermo<<<nsys, TILE, 0, s>>>(D, count_step);
     launched();

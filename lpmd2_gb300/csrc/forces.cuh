@@ -288,20 +288,22 @@ __device__ __forceinline__ void thermo_record(const Dev& D, int s, const double*
   }
 }
 
-// Tail of a mixed force evaluation (one block for every system): the thermo records from the
-// int64 accumulators and, inside a step sequence, the next step's rebuild decision and graph
-// conditional -- one launch instead of a k_thermo and a k_decide.
-__global__ void __launch_bounds__(256) k_tail(Dev D, int count_step, int decide_next, unsigned long long cond_next) {
-  __shared__ int any;
-  if (threadIdx.x == 0) any = 0;
-  __syncthreads();
-  for (int s = threadIdx.x; s < D.nsys; s += blockDim.x) {
+// Tail of a mixed force evaluation, one thread per system: the thermo records from the int64
+// accumulators and, inside a step sequence, the next step's rebuild decision and graph
+// conditional -- one launch instead of a k_thermo and a k_decide.  The conditional starts every
+// graph launch at 0 (cudaGraphCondAssignDefault), so a block raises it only when one of its
+// systems rebuilds and no block ever lowers it.
+constexpr int TAIL_THREADS = 128;
+__global__ void __launch_bounds__(TAIL_THREADS) k_tail(Dev D, int count_step, int decide_next,
+                                                       unsigned long long cond_next) {
+  const int s = blockIdx.x * TAIL_THREADS + threadIdx.x;
+  int need = 0;
+  if (s < D.nsys) {
     if (D.sysd[s].active) thermo_record(D, s, nullptr, count_step);
-    if (decide_next && decide_system(D, s, 2, 0)) atomicOr(&any, 1);
+    if (decide_next) need = decide_system(D, s, 2, 0);
   }
-  __syncthreads();
-  if (threadIdx.x == 0 && decide_next && cond_next)
-    cudaGraphSetConditional((cudaGraphConditionalHandle)cond_next, any ? 1u : 0u);
+  if (__syncthreads_or(need) && threadIdx.x == 0 && cond_next)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)cond_next, 1u);
 }
 
 // Resident blocks per SM the register allocation of the mixed force kernel is sized for.

@@ -78,15 +78,15 @@ __device__ __forceinline__ int decide_system(const Dev& D, int s, int ucall_inc,
   return need;
 }
 
-__global__ void k_decide(Dev D, int nsys, int ucall_inc, int force_all, unsigned long long cond_handle,
-                         int use_cond) {
-  __shared__ int any;
-  if (threadIdx.x == 0) any = 0;
-  __syncthreads();
-  for (int s = threadIdx.x; s < nsys; s += blockDim.x)
-    if (decide_system(D, s, ucall_inc, force_all)) atomicOr(&any, 1);
-  __syncthreads();
-  if (use_cond && threadIdx.x == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)cond_handle, any ? 1u : 0u);
+// One thread per system.  Inside a graph the conditional of the step starts at 0 at every graph
+// launch (cudaGraphCondAssignDefault): a block raises it when one of its systems rebuilds.
+constexpr int DECIDE_THREADS = 128;
+__global__ void __launch_bounds__(DECIDE_THREADS) k_decide(Dev D, int nsys, int ucall_inc, int force_all,
+                                                           unsigned long long cond_handle, int use_cond) {
+  const int s = blockIdx.x * DECIDE_THREADS + threadIdx.x;
+  const int need = s < nsys ? decide_system(D, s, ucall_inc, force_all) : 0;
+  if (__syncthreads_or(need) && use_cond && threadIdx.x == 0)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)cond_handle, 1u);
 }
 
 // ---------------------------------------------------------------------------------------------

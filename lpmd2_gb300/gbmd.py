@@ -537,6 +537,10 @@ class Batch:
         _check(self.lib.gbmd_batch_stats(self.h, ctypes.byref(s)))
         return _stats_dict(s)
 
+    def kernel_times(self) -> dict:
+        """Simulation.kernel_times for the batch (set_option("time_kernels", 1) first)."""
+        return _kernel_times(self.stats())
+
     @property
     def stream(self) -> int:
         p = _VP()

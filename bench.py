@@ -268,10 +268,12 @@ def main():
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
     ap.add_argument("--eam-drift-steps", type=int, default=5000,
                     help="NVE steps of the Sutton-Chen drift comparison, both paths (0: skip)")
-    ap.add_argument("--serve-jobs", type=int, default=32, help="jobs of the served stream (0: skip)")
+    ap.add_argument("--serve-jobs", type=int, default=200, help="jobs of the served stream (0: skip)")
+    ap.add_argument("--budget-burst", type=int, default=80,
+                    help="2,048,000-atom jobs of the burst that presses the 150 GB budget (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate, jobs/s")
-    ap.add_argument("--serve-sweep", default="10,20,50,100,200,500",
-                    help="arrival rates (jobs/s) of the latency sweep, comma-separated ('' to skip)")
+    ap.add_argument("--serve-sweep", default="10,100,500",
+                    help="arrival rates (jobs/s) of the latency sweep, comma-separated ('' to skip; one GPU only)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -300,36 +302,42 @@ def main():
         w_melt = dict(w, pos=p_melt, vel=v_melt)
     sim = make_sim(w_melt, "mixed", device=local)
     sim.update_forces()
-    sim.do_steps(args.warmup)
+    # at least one whole graph block: the CUDA graph of a block is captured at its first use,
+    # which must not fall inside the timed region
+    sim.do_steps(max(args.warmup, GRAPH_BLOCK))
     sim.synchronize()
 
-    def timed_blocks(s, k_total):
-        """k_total steps in graph blocks, CUDA events on the simulation's stream around each
-        block.  No L2 flush: a step streams more than the 129 MB L2 holds (WORKING_SET_NOTE),
-        the same treatment as the end-to-end run.  Returns summed device time in ms."""
+    def timed_steps(s, k):
+        """k steps in ONE call (the library launches its 10-step graphs back to back), CUDA
+        events on the simulation's stream around it.  No L2 flush: a step streams more than the
+        129 MB L2 holds (WORKING_SET_NOTE), the same treatment as the end-to-end run."""
         st = torch.cuda.ExternalStream(s.stream, device=local)
-        ms = 0.0
-        done = 0
-        while done < k_total:
-            b = min(GRAPH_BLOCK, k_total - done)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            s.do_steps(b)
-            e1.record(st)
-            e1.synchronize()
-            ms += e0.elapsed_time(e1)
-            done += b
-        return ms
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s.do_steps(k)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
 
-    stats0 = sim.stats()
-    barrier(dist)
-    torch.cuda.synchronize()
+    def busy(s, seconds):
+        """Untimed steps of the same work for about `seconds` (nvidia-smi samples every 200 ms, a
+        20-step timed region lasts a few ms: the samples around it describe its clocks)."""
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            s.do_steps(GRAPH_BLOCK * 10)
+            s.synchronize()
+
     with ClockSampler(local) as clk:
-        ms = timed_blocks(sim, args.steps)
-    torch.cuda.synchronize()
-    barrier(dist)
-    stats1 = sim.stats()
+        busy(sim, 0.7)
+        stats0 = sim.stats()
+        barrier(dist)
+        torch.cuda.synchronize()
+        ms = timed_steps(sim, args.steps)
+        torch.cuda.synchronize()
+        barrier(dist)
+        stats1 = sim.stats()
+        busy(sim, 0.4)
     ms = allmax(dist, ms)
     value = N * args.steps * world / (ms * 1e-3)
 
@@ -338,7 +346,7 @@ def main():
     sim64.update_forces()
     k64 = max(GRAPH_BLOCK, (args.steps // 5) // GRAPH_BLOCK * GRAPH_BLOCK)
     sim64.do_steps(GRAPH_BLOCK)
-    ms64 = timed_blocks(sim64, k64)
+    ms64 = timed_steps(sim64, k64)
     value64 = N * k64 / (ms64 * 1e-3)
 
     # error of the mixed forces against FP64 at identical positions
@@ -377,7 +385,9 @@ def main():
     batched = batched_ensemble(local, args.batch_steps, rank=rank, world=world, dist=dist) if args.batch_steps > 0 else None
     served = served_stream(local, args.serve_jobs, args.serve_rate, rank, world, dist) if args.serve_jobs > 0 else None
     sweep = []
-    if args.serve_jobs > 0 and args.serve_sweep.strip():
+    sc_rate = sc_batched_rate(local) if args.serve_jobs > 0 and world == 1 else None
+    burst = budget_burst(local, args.budget_burst) if args.budget_burst > 0 and world == 1 else None
+    if args.serve_jobs > 0 and args.serve_sweep.strip() and world == 1:
         for rate in (float(x) for x in args.serve_sweep.split(",")):
             r = served if rate == args.serve_rate else served_stream(local, args.serve_jobs, rate, rank, world, dist)
             sweep.append({"rate_jobs_per_s": rate, "p50_latency_s": r["p50_latency_s"],
@@ -400,6 +410,9 @@ def main():
                    "graph_block": GRAPH_BLOCK, "melt_steps": args.melt, "melt_precision": "fp64", "seed": 2,
                    "rng": "SplitMix64 (lpmd2_gb300/inputs.py)",
                    "l2": WORKING_SET_NOTE,
+                   "warmup_note": "at least one 10-step graph block untimed (the graph is captured there), "
+                                  "and about 1 s of untimed steps of the same work around the timed region "
+                                  "while nvidia-smi samples the clocks",
                    "parallelism": f"replicas x{world}"},
         "ns_per_day": value / N / world * w["dt"] * 86400 * 1e-6,
         "gpu_launches": launches,
@@ -409,6 +422,8 @@ def main():
         "batched": batched,
         "served": served,
         "served_sweep": sweep or None,
+        "served_budget_burst": burst,
+        "sc_batched": sc_rate,
         "eam": eam,
         "drift": drift_cmp,
         "kernel_ms": kt,
@@ -420,7 +435,7 @@ def main():
         "virial_rel_err_vs_fp64": abs(w_m - w_64) / abs(w_64),
         "speedup_vs_fp64": value / (value64 * world),
         "summary": summarize_line(value, value64 * world, e2e, frel, abs(e_m - e_64) / abs(e_64),
-                                  abs(w_m - w_64) / abs(w_64), drift_cmp, eam, batched, served),
+                                  abs(w_m - w_64) / abs(w_64), drift_cmp, eam, batched, served, sc_rate, burst),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic,
                      "traffic_source": "not measured in this run: dram__bytes_read.sum + dram__bytes_write.sum "
@@ -437,7 +452,8 @@ def main():
     print(json.dumps(out))
 
 
-def summarize_line(value, value64, e2e, frel, erel, wrel, drift, eam, batched, served) -> dict:
+def summarize_line(value, value64, e2e, frel, erel, wrel, drift, eam, batched, served, sc_rate=None,
+                   burst=None) -> dict:
     """The benchmark's headline figures in one short object: the mixed/FP64 ratio with its
     errors for each workload, NVE drift, and the served stream's latency against the batched
     engine's throughput."""
@@ -464,8 +480,16 @@ def summarize_line(value, value64, e2e, frel, erel, wrel, drift, eam, batched, s
     if served:
         out["served"] = {"p50_s": r(served["p50_latency_s"], 3), "p99_s": r(served["p99_latency_s"], 3),
                          "atom_steps_per_s": r(served["atom_steps_per_s"]), "jobs": served["completed"]}
-        if batched:
-            out["served"]["fraction_of_batched"] = r(served["atom_steps_per_s"] / batched["value"], 3)
+        if batched and sc_rate:
+            # the batched engine's rate for the same work: LJ at the ensemble's rate, copper at the
+            # copper batch's, weighted by the stream's atom-steps of each kind
+            wk = served["atom_steps_by_kind"]
+            ideal = (wk["lj"] + wk["sc"]) / (wk["lj"] / batched["value"] + wk["sc"] / sc_rate["value"])
+            out["served"]["batched_rate_same_mix"] = r(ideal)
+            out["served"]["fraction_of_batched_same_mix"] = r(served["atom_steps_per_s"] / ideal, 3)
+    if burst:
+        out["budget_burst"] = {"peak_gb": r(burst["peak_budget_used_bytes"] / 1e9, 4), "jobs": burst["completed"],
+                               "batches": burst["batches"]}
     return out
 
 
@@ -602,26 +626,20 @@ def make_batch(systems, precision: str, device: int, params: dict):
 
 
 def time_batch(b, device: int, warm: int, steps: int) -> float:
-    """Device ms of `steps` steps in graph blocks on the batch's stream (events around each
-    block), after `warm` untimed steps."""
+    """Device ms of `steps` steps in one call on the batch's stream (events around it), after
+    `warm` untimed steps (at least one graph block, so the graph is captured before)."""
     import torch
 
     b.update_forces()
-    b.do_steps(warm)
+    b.do_steps(max(warm, GRAPH_BLOCK))
     st = torch.cuda.ExternalStream(b.stream, device=device)
-    ms = 0.0
-    done = 0
-    while done < steps:
-        k = min(GRAPH_BLOCK, steps - done)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        b.do_steps(k)
-        e1.record(st)
-        e1.synchronize()
-        ms += e0.elapsed_time(e1)
-        done += k
-    return ms
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.do_steps(steps)
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
 
 
 def batched_ensemble(device: int, steps: int, nsys: int = 512, rank: int = 0, world: int = 1, dist=None) -> dict:
@@ -686,9 +704,60 @@ def served_stream(device: int, njobs: int, rate: float, rank: int = 0, world: in
         res = [JobResult(0, "", n, st, a, finished=f, error=e) for part in gathered for (n, st, a, f, e) in part]
         wall = allmax(dist, wall)
     out = summarize(res, wall)
+    work = {"lj": 0, "sc": 0}
+    for j in everything:
+        work[j["kind"]] += 4 * j["k"] ** 3 * j["steps"]
     out.update({"rate_jobs_per_s": rate, "seed": 5, "budget_bytes": 150e9, "batches": srv.batches_started,
-                "peak_budget_used_bytes": srv.peak_used,
+                "peak_budget_used_bytes": srv.peak_used, "atom_steps_by_kind": work,
                 "note": "latency = completion - arrival, wall clock; payloads generated before the clock starts"})
+    return out
+
+
+def sc_batched_rate(device: int, nsys: int = 48, steps: int = 40) -> dict:
+    """The batched engine's rate on Sutton-Chen copper systems of the served stream's sizes (FCC
+    k^3 cells, k of the stream's copper jobs), with the job server's plugins: the copper half of
+    the reference the served throughput is compared with."""
+    from lpmd2_gb300 import gbmd
+    from lpmd2_gb300 import inputs as I
+    from lpmd2_gb300.serve import GbmdBackend
+
+    jobs = [j for j in I.job_stream(4 * nsys, 100.0, seed=5) if j["kind"] == "sc"][:nsys]
+    systems = [I.materialize_job(j) for j in jobs]
+    be = GbmdBackend(device=device)
+    b = gbmd.Batch([s["natoms"] for s in systems], [s["L"] for s in systems], device=device)
+    for k, sy in enumerate(systems):
+        b.set_atoms(k, sy["pos"], sy["vel"], Z=sy["Z"], mass=sy["mass"])
+    cm, pot, integ = be.plugins("sc")
+    b.set_cell_manager(cm)
+    b.add_potential(pot)
+    b.set_integrator(integ)
+    b.set_precision("mixed")
+    b.set_option("graph_block", GRAPH_BLOCK)
+    ms = time_batch(b, device, 20, steps)
+    b.close()
+    natoms = sum(sy["natoms"] for sy in systems)
+    return {"systems": nsys, "natoms": natoms, "steps": steps, "value": natoms * steps / (ms * 1e-3),
+            "unit": "atom-steps/s"}
+
+
+def budget_burst(device: int, njobs: int = 80, k: int = 80, steps: int = 50) -> dict:
+    """A burst of large LJ jobs (FCC k^3 = 2,048,000 atoms each, rho* 0.8, T* 1.2, `steps` steps,
+    all arriving at once) whose footprints add up to more than the 150 GB budget: the server
+    admits as many as fit and the rest wait for memory.  Every job carries the same payload
+    (made once, before the clock starts)."""
+    from lpmd2_gb300 import inputs as I
+    from lpmd2_gb300.serve import GbmdBackend, Server, summarize
+
+    payload = I.lj_system(k, 0.8, 1.2, seed=51)
+    jobs = [dict(id=q, kind="lj", k=k, steps=steps, arrival=0.0) for q in range(njobs)]
+    srv = Server(GbmdBackend(device=device), budget_bytes=150e9, max_batches=8, max_systems=512)
+    t0 = time.perf_counter()
+    res = srv.serve(jobs, lambda j: payload)
+    wall = time.perf_counter() - t0
+    out = summarize(res, wall)
+    out.update({"jobs_atoms_each": payload["natoms"], "steps_each": steps, "budget_bytes": 150e9,
+                "peak_budget_used_bytes": srv.peak_used, "batches": srv.batches_started,
+                "note": "all jobs arrive at t = 0; admission against the budget"})
     return out
 
 

@@ -1298,7 +1298,7 @@ struct Engine::Impl {
     if (mixed) {
       k_kinetic_slots_clear<<<1, 256, 0, stream>>>(D);
       k_step_kinetic<1><<<ntiles, TILE, 0, stream>>>(D);
-      k_tail<<<1, 256, 0, stream>>>(D, 1, 0, 0ull);
+      k_tail<<<nblocks(nsys, TAIL_THREADS), TAIL_THREADS, 0, stream>>>(D, 1, 0, 0ull);
       launched(3);
     } else {
       k_step_kinetic<0><<<ntiles, TILE, 0, stream>>>(D);

@@ -262,7 +262,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short direct-launch run of the workload for ncu (no timing, no JSON)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
-    ap.add_argument("--workload", default="lj", choices=["lj", "eam"], help="with --profile")
+    ap.add_argument("--workload", default="lj", choices=["lj", "eam", "ensemble", "ensemble-small"],
+                    help="with --profile: the LJ liquid, the Sutton-Chen copper, the 512-system ensemble, or 512 "
+                         "systems of 256 atoms (FCC 4^3, the ensemble's smallest size)")
     ap.add_argument("--drift-steps", type=int, default=10000, help="NVE steps of the drift comparison")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched ensemble (0: skip)")
     ap.add_argument("--eam-steps", type=int, default=100, help="timed steps of the Sutton-Chen Cu system (0: skip)")
@@ -497,6 +499,23 @@ def run_profile(args):
     """The workload with direct launches only (graph_mode 0), for ncu: melt, warm up, then
     --steps steps.  Every kernel of a step is a separate launch on the simulation's stream.
     --workload eam profiles the Sutton-Chen copper system instead of the LJ liquid."""
+    if args.workload in ("ensemble", "ensemble-small"):
+        from lpmd2_gb300 import inputs as I
+
+        if args.workload == "ensemble":
+            systems = I.lj_ensemble(512, seed=4)
+        else:
+            systems = [I.lj_system(4, 0.70 + 0.25 * (q % 7) / 6, 0.7 + 1.3 * (q % 5) / 4, seed=900 + q)
+                       for q in range(512)]
+        b = make_batch(systems, args.precision, 0, {"skin_sigma": 0.3, "cell_scale": 1, "lanes_per_atom": 1})
+        b.set_option("graph_mode", 0)
+        b.update_forces()
+        b.do_steps(args.melt + args.warmup)
+        b.do_steps(args.steps)
+        b.synchronize()
+        print(json.dumps({"profile": True, "workload": args.workload, "systems": len(systems),
+                          "natoms": sum(q["natoms"] for q in systems), "steps": args.steps, **b.stats()}))
+        return
     if args.workload == "eam":
         sim, natoms = make_eam_sim(args.precision)
         sim.set_option("graph_mode", 0)

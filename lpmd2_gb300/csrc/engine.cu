@@ -899,12 +899,19 @@ struct Engine::Impl {
       sp.kinetic = 1;
       sp.raw_acc = raw;
       const int mode = sysd[0].mode;
+      const bool species = P.spc_sum >= 0;
+      // Sutton-Chen exponent pairs of common metals get straight-line powers, and without a
+      // species filter the many-body prefactor folded into the gathered embedding factor
+      const bool sc96 = P.kind == POT_SC && P.int_n == 9 && P.int_m == 6;
+      const bool sc126 = P.kind == POT_SC && P.int_n == 12 && P.int_m == 6;
+      PotParams Pe = P;
+      Pe.f[14] = (!species && (sc96 || sc126)) ? P.f[2] : 1.0f;  // scale of the density pass's copy
       if (!pair_kind(P.kind)) {
         int first = (p == first_eam);
         if (mixed && P.kind == POT_SC && P.int_m == 6)
-          k_eam_density32<6><<<ntiles, TILE, 0, s>>>(D, P);
+          k_eam_density32<6><<<ntiles, TILE, 0, s>>>(D, Pe);
         else if (mixed)
-          k_eam_density32<0><<<ntiles, TILE, 0, s>>>(D, P);
+          k_eam_density32<0><<<ntiles, TILE, 0, s>>>(D, Pe);
         else if (mode == NB_LIST)
           k_eam_density<NB_LIST><<<ntiles, TILE, 0, s>>>(D, P, first);
         else if (mode == NB_CELLS)
@@ -914,7 +921,6 @@ struct Engine::Impl {
         launched();
       }
       if (mixed) {
-        const bool species = P.spc_sum >= 0;
         if (pair_kind(P.kind) && lanes > 1) {
           const unsigned g = (unsigned)ntiles * lanes;
           if (lanes == 2)
@@ -933,17 +939,14 @@ struct Engine::Impl {
           else
             k_force32<PC_PAIR, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
         } else {
-          // Sutton-Chen exponent pairs of common metals get straight-line powers
-          const bool sc96 = P.kind == POT_SC && P.int_n == 9 && P.int_m == 6;
-          const bool sc126 = P.kind == POT_SC && P.int_n == 12 && P.int_m == 6;
           if (species)
-            k_force32<PC_EAM, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            k_force32<PC_EAM, 1><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else if (sc96)
-            k_force32<PC_EAM, 0, 9, 6><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            k_force32<PC_EAM, 0, 9, 6><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else if (sc126)
-            k_force32<PC_EAM, 0, 12, 6><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            k_force32<PC_EAM, 0, 12, 6><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else
-            k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
         }
       } else if (mode == NB_LIST) {
         if (pair_kind(P.kind))

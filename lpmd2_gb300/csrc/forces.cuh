@@ -452,7 +452,10 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4 gi = active ? g32[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = __float_as_int(gi.w);
-    const float phi_i = (PC == PC_EAM && active) ? D.phif[i] : 0.f;
+    // the embedding factor as the loop uses it: the density pass's copy (f[14] x 1/sqrt(rho),
+    // f[14] = the Sutton-Chen many-body prefactor in the folded form, else 1) where gathered
+    const float phi_i = (PC == PC_EAM && active) ? (PHI_IN_W ? gsrc[li].w : D.phif[i]) : 0.f;
+    constexpr bool FOLDED = PHI_IN_W && SCN > 0;
     const int na = S.natoms;
     const int cnt = active ? D.ncount[i] : 0;
     const int ng = (cnt + 3) >> 2;
@@ -481,6 +484,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       float g, en;
       if (PC == PC_PAIR) {
         lj_pair32(P, rcp_approx(r2), g, en);
+      } else if constexpr (FOLDED) {
+        eam_sc_pair32_q<SCN, SCM>(P, r2, phi_i, gj.w, g, en);
       } else {
         eam_pair32_t<SCN, SCM>(P, r2, phi_i, PHI_IN_W ? gj.w : D.phif[S.atom_base + j], g, en);
       }
@@ -575,7 +580,8 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
         if (PC == PC_PAIR) {
           lj_pair32(P, rcp_approx(r2), g, en);
         } else {
-          eam_pair32_t<SCN, SCM>(P, r2, phi_i, D.phif[S.atom_base + j], g, en);
+          // the unscaled embedding factors of both atoms (rare path)
+          eam_pair32_t<SCN, SCM>(P, r2, D.phif[i], D.phif[S.atom_base + j], g, en);
         }
         const float fx = g * dx, fy = g * dy, fz = g * dz;
         fqx.add_scaled32(fx);
@@ -934,7 +940,7 @@ __global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
     D.rho[i] = rho;
     D.phi[i] = phi;
     D.phif[i] = (float)phi;
-    D.g32e[i] = make_float4(gi.x, gi.y, gi.z, (float)phi);
+    D.g32e[i] = make_float4(gi.x, gi.y, gi.z, (float)((double)P.f[14] * phi));
   }
   // FP64 embedding energies summed exactly as int64 fixed point (2^-32 eV per atom)
   long long v[1] = {active ? __double2ll_rn(F * FIX_E) : 0ll};

@@ -370,6 +370,11 @@ __device__ __forceinline__ int shift_code(int kx, int ky, int kz) { return (kx +
 // divergence between lanes, since all atoms of a cell share the stencil and its cell-shift
 // codes), and appends its hits in candidate order through a bit mask.
 constexpr int LIST_WARPS = 4;
+// Candidate tests four at a time over a sentinel-padded stage, appends through a running write
+// position (1); or one candidate per iteration with the entry address recomputed per append (0).
+#ifndef GBMD_LIST_UNROLL4
+#define GBMD_LIST_UNROLL4 1
+#endif
 // Resident blocks per SM the register allocation of the list build is sized for.
 #ifndef GBMD_LIST_MIN_BLOCKS
 #define GBMD_LIST_MIN_BLOCKS 4
@@ -413,6 +418,9 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
     unsigned* out = nl + (long long)li * 4;
     const long long gstride = (long long)na * 4;  // words between consecutive groups of four
     int cnt = 0;
+#if GBMD_LIST_UNROLL4
+    unsigned* wp = out;
+#endif
     for (int dz = -R; dz <= R; ++dz) {
       const int zc = wrap_around(cz + dz, nz);
       const float sz = (float)dz * dfz;
@@ -428,25 +436,51 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
           const float ox = sx - gi.x, oy = sy - gi.y, oz = sz - gi.z;
           for (int jb = 0; jb < n; jb += 32) {
             __syncwarp();
+#if GBMD_LIST_UNROLL4
+            // every stage slot is written: past the cell's atoms a far-away sentinel, so the test
+            // loop runs in whole quads of candidates (the sentinel never hits: r^2 ~ 3e36)
+            st[lane] = jb + lane < n ? g32[b + jb + lane] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+#else
             if (jb + lane < n) st[lane] = g32[b + jb + lane];
+#endif
             __syncwarp();
             const int m = min(32, n - jb);
             const int jl0 = b + jb - (int)atom_base;
             // pass 1: a bit per staged candidate inside the list radius (branch-free)
             unsigned hits = 0u;
+#if GBMD_LIST_UNROLL4
+            for (int k = 0; k < m; k += 4) {
+              unsigned nib = 0u;
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const float4 gj = st[k + u];
+                const float rx = ox + gj.x, ry = oy + gj.y, rz = oz + gj.z;
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                nib |= (r2 < rl2 ? 1u : 0u) << u;
+              }
+              hits |= nib << k;
+            }
+#else
             for (int k = 0; k < m; ++k) {
               const float4 gj = st[k];
               const float rx = ox + gj.x, ry = oy + gj.y, rz = oz + gj.z;
               const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
               hits |= (r2 < rl2 ? 1u : 0u) << k;
             }
+#endif
             const int self = li - jl0;  // drop the atom itself
             if (self >= 0 && self < 32) hits &= ~(1u << self);
             // pass 2: append the hits in candidate order
             while (hits) {
               const int k = __ffs(hits) - 1;
               hits &= hits - 1u;
+#if GBMD_LIST_UNROLL4
+              // running write position: entry cnt of the atom lives at group cnt/4, slot cnt%4
+              if (cnt < maxnb) *wp = code | (unsigned)(jl0 + k);
+              wp += (cnt & 3) == 3 ? gstride - 3 : 1;
+#else
               if (cnt < maxnb) out[(cnt >> 2) * gstride + (cnt & 3)] = code | (unsigned)(jl0 + k);
+#endif
               ++cnt;
             }
           }

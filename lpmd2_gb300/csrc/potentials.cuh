@@ -177,6 +177,8 @@ __device__ __forceinline__ void eam_pair64(const PotParams& P, double r, double 
 //   SC: f[0]=e*an, f[1]=-n*e*an, f[2]=0.5*m*c*e*am, f[3]=am
 //   FS/FSX: f[0..4]=c0..c4, f[5]=A, f[6]=B, f[7]=c, f[8]=d
 //   Gupta: f[0]=A, f[1]=-p/r0, f[2]=-A p/r0, f[3]=B q/r0, f[4]=-2q/r0, f[5]=r0
+//   all EAM, set per launch: f[14] = the factor the density pass applies to the embedding factor
+//   it stores beside the position (f[2] for the folded Sutton-Chen form, else 1)
 // ------------------------------------------------------------------------------------------
 
 // g with F_i = g * r_ij, and the pair energy e; inv = 1/r^2.  sigma^2 enters as the double-float
@@ -279,6 +281,21 @@ __device__ __forceinline__ float eam_rho32_t(const PotParams& P, float r2) {
   } else {
     return eam_rho32(P, r2);
   }
+}
+
+// Sutton-Chen with compile-time n = N, m = M and the many-body prefactor folded into the
+// embedding factors: qi = f[2] / sqrt(rho_i) (and qj), so s = f[1] r^-(N+2) + (qi + qj) r^-(M+2)
+// and e = f[0] r^-N, every power built from 1/r^2 and one refined 1/r.
+template <int N, int M>
+__device__ __forceinline__ void eam_sc_pair32_q(const PotParams& P, float r2, float qi, float qj, float& s,
+                                                float& e) {
+  static_assert(M % 2 == 0, "the folded form takes even m");
+  const float ir = rsqrt_nr(r2);
+  const float inv = ir * ir;
+  const float pm = ipow_c<(M + 2) / 2>(inv);                                  // r^-(M+2)
+  const float pn = (N % 2 == 0) ? ipow_c<N / 2>(inv) : ipow_c<N / 2>(inv) * ir;  // r^-N
+  e = P.f[0] * pn;
+  s = fmaf(P.f[1], pn * inv, (qi + qj) * pm);
 }
 
 template <int N, int M>

@@ -691,12 +691,21 @@ def batched_ensemble(device: int, steps: int, nsys: int = 512, rank: int = 0, wo
     ms, ms64 = allmax(dist, ms), allmax(dist, ms64)
     value = total_atoms * steps / (ms * 1e-3)
     value64 = total_atoms * k64 / (ms64 * 1e-3)
+    # the other end of the size range: 512 systems of the ensemble's smallest size (FCC 4^3,
+    # 256 atoms), where launches per step and the rebuild chain weigh most against the work
+    small = [I.lj_system(4, 0.70 + 0.25 * (q % 7) / 6, 0.7 + 1.3 * (q % 5) / 4, seed=900 + q) for q in range(nsys)]
+    bs = make_batch(small, "mixed", device, dict(best, lanes_per_atom=1))
+    ms_small = time_batch(bs, device, 20, steps)
+    bs.close()
+    small_atoms = sum(q["natoms"] for q in small)
     return {"workload": f"lj_ensemble_{nsys}", "seed": 4, "systems": nsys, "natoms_total": total_atoms,
             "systems_this_rank": len(systems), "natoms_this_rank": natoms,
             "natoms_min": min(s["natoms"] for s in everything), "natoms_max": max(s["natoms"] for s in everything),
             "steps": steps, "value": value, "unit": "atom-steps/s", "ms_per_step": ms / steps,
             "fp64_value": value64, "speedup_vs_fp64": value / value64, "tuned": best, "tuning_trials": trials,
             "tuning_s": tune_s, "device_bytes": st["device_bytes"],
+            "small_systems": {"systems": nsys, "natoms_each": 256, "ms_per_step": ms_small / steps,
+                              "value": small_atoms * steps / (ms_small * 1e-3)},
             "launch": "one launch per kernel for all systems; 10-step blocks as one CUDA graph"}
 
 
@@ -812,8 +821,20 @@ def eam_metal(device: int, steps: int, drift_steps: int = 5000, ncell: int = 50)
     w = I.sc_cu_system(ncell, seed=3)
     N = w["natoms"]
 
+    # the device's Verlet skin (linkedcell leaves it to the device), chosen by timing
+    from lpmd2_gb300.autotune import tune_skin
+
+    def with_skin(skin):
+        sim = make_eam_sim("mixed", device, w, ncell)[0]
+        sim.set_option("skin", skin)
+        return sim
+
+    skin, skin_trials = tune_skin(with_skin, lambda sim: time_batch(sim, device, 30, 150) / 150)
+
     def make(prec, state):
-        return make_eam_sim(prec, device, state, ncell)[0]
+        sim = make_eam_sim(prec, device, state, ncell)[0]
+        sim.set_option("skin", skin)
+        return sim
 
     def errors(state) -> dict:
         sm, s64 = make("mixed", state), make("fp64", state)
@@ -853,6 +874,7 @@ def eam_metal(device: int, steps: int, drift_steps: int = 5000, ncell: int = 50)
            "unit": "atom-steps/s", "ms_per_step": ms / steps, "ns_per_day": value / N * 2.0 * 86400 * 1e-6,
            "fp64_value": value64, "speedup_vs_fp64": value / value64,
            "errors_20_fp64_steps": err20, "errors_after_timed_run": dict(err_hot, at=f"after {20 + steps} mixed steps"),
+           "skin_a": skin, "skin_trials": skin_trials,
            "neighbor_mode": st["neighbor_mode"], "list_radius": st["list_radius"]}
     if drift_steps > 0:
         out["drift"] = nve_drift(lambda prec: make(prec, w), N, 2.0, drift_steps)

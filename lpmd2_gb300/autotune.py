@@ -42,3 +42,25 @@ def tune_batch(make: Callable[[dict], object], ms_per_step: Callable[[object], f
             trial({"skin_sigma": best["skin_sigma"], "cell_scale": best["cell_scale"], "lanes_per_atom": int(ln)})
     best = min(trials, key=lambda t: t["ms_per_step"])
     return {k: best[k] for k in ("skin_sigma", "cell_scale", "lanes_per_atom")}, trials
+
+
+# Verlet skins (A) tried for a single system whose cell manager leaves the skin to the device
+# (linkedcell: the reference has no skin; the device's list adds one).  For Sutton-Chen copper
+# at 300 K (495,000 atoms, cutoff 7.22 A) the GB300 times per step, rebuilds included, were
+# 0.532 / 0.509 / 0.509 / 0.533 / 0.538 / 0.571 ms at 0.2 / 0.3 / 0.4 / 0.5 / 0.722 / 1.0 A.
+SKINS_A = (0.3, 0.4, 0.5, 0.722)
+
+
+def tune_skin(make: Callable[[float], object], ms_per_step: Callable[[object], float],
+              skins=SKINS_A) -> tuple[float, list[dict]]:
+    """make(skin) builds a simulation with that Verlet skin; ms_per_step(sim) times it (rebuilds
+    included, so over enough steps to see several).  Returns the fastest skin and every trial."""
+    trials = []
+    for skin in skins:
+        sim = make(float(skin))
+        try:
+            trials.append({"skin": float(skin), "ms_per_step": float(ms_per_step(sim))})
+        finally:
+            sim.close()
+    return min(trials, key=lambda t: t["ms_per_step"])["skin"], trials
+

@@ -1,5 +1,5 @@
 """The autotuner's selection logic on the CPU with a stand-in batch."""
-from lpmd2_gb300.autotune import CELL_SCALES, LANES_PER_ATOM, SKINS_SIGMA, tune_batch
+from lpmd2_gb300.autotune import CELL_SCALES, LANES_PER_ATOM, SKINS_A, SKINS_SIGMA, tune_batch, tune_skin
 
 
 class Stub:
@@ -35,3 +35,12 @@ def test_trial_failure_still_closes():
     except RuntimeError:
         pass
     assert len(closed) == 1 and closed[0].closed
+
+
+def test_skin_tuner_picks_fastest_and_closes():
+    closed = []
+    best, trials = tune_skin(lambda k: Stub({"skin": k}, closed), lambda b: 1.0 + abs(b.p["skin"] - 0.4))
+    assert best == 0.4
+    assert [t["skin"] for t in trials] == list(SKINS_A) and len(closed) == len(SKINS_A)
+    assert all(s.closed for s in closed)
+

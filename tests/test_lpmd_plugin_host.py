@@ -1,10 +1,17 @@
-"""The LPMD-side binding, host side: lpmd2_gb300/lpmd_plugin/gbmd.cc compiled against the
-reference's liblpmd headers and loaded through liblpmd's own PluginLoader (the reference's
+"""The LPMD-side binding, host side: the plugins of lpmd2_gb300/lpmd_plugin/ compiled against
+the reference's liblpmd headers and loaded through liblpmd's own PluginLoader (the reference's
 sources, built by oracle/Makefile's `ref` target), in a process that has no GPU.
 
-Checks that the plugin is an lpmd::Integrator reachable by dynamic_cast, that its keywords and
-defaults are processed by Module::ProcessArguments, and that a keyword without a value raises
-the reference's SyntaxError.  Skipped where the reference checkout or its build is absent.
+The `gbmd` integrator plugin (gbmd.cc): an lpmd::Integrator reachable by dynamic_cast, its
+keywords and defaults processed by Module::ProcessArguments, a keyword without a value raising
+the reference's SyntaxError.
+
+The GPU plugins under LPMD's own names (plugins.cc, one .so per name): loaded beside the
+reference plugin of the same name, each is the same kind of object with the same keywords and
+defaults; the host functionals (pairEnergy, pairForce, rhoij, F, PairForce, ManyBodies) equal
+the reference's bit for bit; and a simulation wired through liblpmd (SetCellManager,
+UpdateForces, DoStep, BuildNeighborList) reaches libgbmd, whose "no CUDA device" status comes
+back as lpmd::RuntimeError.  Skipped where the reference checkout or its build is absent.
 """
 import os
 import subprocess

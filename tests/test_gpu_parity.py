@@ -135,10 +135,16 @@ def test_mixed_forces_and_neighbors(case):
     th = sim.thermo_raw()
     assert rms_err(acc, g["acc0"]) <= 1e-5 * force_scale(g)
     assert abs(th[1] - g["thermo0"][1]) <= 1e-6 * abs(g["thermo0"][1])
-    # On a perfect lattice every pair of a shell has the same FP32 rounding, so the errors of
-    # the ~1e5 virial terms add up instead of averaging out (2e-5 measured on lj_ar_fcc10);
-    # at thermalised states the virial meets 1e-5 (test_forces_at_thermalised_state).
-    assert abs(th[5] - g["thermo0"][5]) <= 1e-4 * abs(g["thermo0"][5])
+    # These are the cases' initial states, lattices or near-lattices, where every pair of a
+    # shell has the same FP32 rounding, so the errors of the ~1e5 virial terms add up instead of
+    # averaging out.  Measured on the GB300 (relative virial error): lj_ar_fcc10 2.6e-7,
+    # lj_liquid_vl 6.8e-8, fs_fe 1.9e-7, fsx_mo 2.5e-6, gupta_au 5.8e-8, sc_cu 1.8e-5.  The
+    # Sutton-Chen lattice at a = 3.61 A is close to its equilibrium spacing: pair repulsion and
+    # many-body attraction cancel to a small residual there, and the coherent rounding of each
+    # shell's terms is amplified by that cancellation.  At thermalised states every case meets
+    # 1e-5 (test_forces_at_thermalised_state), the 495k copper included (test_gpu_fullsize.py).
+    tol_w = 3e-5 if case == "sc_cu" else 1e-5
+    assert abs(th[5] - g["thermo0"][5]) <= tol_w * abs(g["thermo0"][5])
     check_neighbors(sim, g)
     assert sim.stats()["neighbor_mode"] == "verlet"
 

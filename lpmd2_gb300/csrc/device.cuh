@@ -391,6 +391,43 @@ __device__ __forceinline__ float rcp_nr(float x) {
   return fmaf(y, fmaf(-x, y, 1.0f), y);
 }
 
+// Two FP32 values in one 64-bit register pair, operated on by the packed .f32x2 instructions
+// (sm_100 and later): one instruction issue for two IEEE round-to-nearest results, each half
+// rounded exactly as the scalar instruction rounds it, so a packed computation that keeps the
+// scalar operation order gives bit-identical values.  GBMD_F32X2=0 selects the scalar forms.
+#ifndef GBMD_F32X2
+#define GBMD_F32X2 1
+#endif
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
 // FP32 displacement and squared distance of a Verlet-list entry: cell shift of the entry's
 // code plus the difference of the cell-relative offsets.  The force, density and neighbour
 // export kernels all decide cutoffs on this value, so their pair sets agree bit for bit.
@@ -409,6 +446,19 @@ __device__ __forceinline__ ShiftCorr shift_corr(const SysDev& S) {
 }
 __device__ __forceinline__ float entry_r2(const float4& gi, const float4& gj, const float4& sh, const ShiftCorr& c,
                                           float& dx, float& dy, float& dz) {
+#if GBMD_F32X2
+  // x and y as one packed pair (each float4's x, y sit in an aligned register pair)
+  const f32x2 shxy = f2_pack(sh.x, sh.y);
+  f32x2 dxy = f2_sub(f2_add(shxy, f2_pack(gj.x, gj.y)), f2_pack(gi.x, gi.y));
+#if GBMD_SHIFT_CORR
+  dxy = f2_fma(shxy, f2_pack(c.x, c.y), dxy);
+#endif
+  f2_unpack(dxy, dx, dy);
+  dz = (sh.z + gj.z) - gi.z;
+#if GBMD_SHIFT_CORR
+  dz = fmaf(sh.z, c.z, dz);
+#endif
+#else
   dx = (sh.x + gj.x) - gi.x;
   dy = (sh.y + gj.y) - gi.y;
   dz = (sh.z + gj.z) - gi.z;
@@ -416,6 +466,7 @@ __device__ __forceinline__ float entry_r2(const float4& gi, const float4& gj, co
   dx = fmaf(sh.x, c.x, dx);
   dy = fmaf(sh.y, c.y, dy);
   dz = fmaf(sh.z, c.z, dz);
+#endif
 #endif
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }

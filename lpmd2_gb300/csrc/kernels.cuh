@@ -381,7 +381,13 @@ constexpr int LIST_WARPS = 4;
 #endif
 
 __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_buildlist(Dev D) {
+#if GBMD_LIST_UNROLL4 && GBMD_F32X2
+  // coordinates staged as three arrays, so that one 16-byte shared load gives the x (y, z)
+  // of four consecutive candidates: two packed pairs
+  __shared__ __align__(16) float stage[LIST_WARPS][3][32];
+#else
   __shared__ float4 stage[LIST_WARPS][32];
+#endif
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // every block covers LIST_WARPS cells of one system (a per-block table), so the system
   // index is the same for the whole block and the grid holds no block of an empty range
@@ -408,7 +414,13 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
   const int c = g0 - cell_base;
   const int b0 = cstart[g0], n0 = ccnt[g0];
   const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+#if GBMD_LIST_UNROLL4 && GBMD_F32X2
+  float* const stx = stage[w][0];
+  float* const sty = stage[w][1];
+  float* const stz = stage[w][2];
+#else
   float4* st = stage[w];
+#endif
   for (int base = 0; base < n0; base += 32) {
     const bool has = base + lane < n0;
     const long long i = (long long)b0 + base + lane;
@@ -434,9 +446,19 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
           const int b = cstart[g], n = ccnt[g];
           const unsigned code = (unsigned)shift_code(dx, dy, dz) << CODE_SHIFT;
           const float ox = sx - gi.x, oy = sy - gi.y, oz = sz - gi.z;
+#if GBMD_LIST_UNROLL4 && GBMD_F32X2
+          const f32x2 ox2 = f2_pack(ox, ox), oy2 = f2_pack(oy, oy), oz2 = f2_pack(oz, oz);
+#endif
           for (int jb = 0; jb < n; jb += 32) {
             __syncwarp();
-#if GBMD_LIST_UNROLL4
+#if GBMD_LIST_UNROLL4 && GBMD_F32X2
+            {
+              const float4 gj = jb + lane < n ? g32[b + jb + lane] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+              stx[lane] = gj.x;
+              sty[lane] = gj.y;
+              stz[lane] = gj.z;
+            }
+#elif GBMD_LIST_UNROLL4
             // every stage slot is written: past the cell's atoms a far-away sentinel, so the test
             // loop runs in whole quads of candidates (the sentinel never hits: r^2 ~ 3e36)
             st[lane] = jb + lane < n ? g32[b + jb + lane] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
@@ -448,7 +470,25 @@ __global__ void __launch_bounds__(32 * LIST_WARPS, GBMD_LIST_MIN_BLOCKS) k_build
             const int jl0 = b + jb - (int)atom_base;
             // pass 1: a bit per staged candidate inside the list radius (branch-free)
             unsigned hits = 0u;
-#if GBMD_LIST_UNROLL4
+#if GBMD_LIST_UNROLL4 && GBMD_F32X2
+            for (int k = 0; k < m; k += 4) {
+              // candidates k..k+3 as two packed pairs, in the scalar form's operation order
+              const float4 X = *reinterpret_cast<const float4*>(stx + k);
+              const float4 Y = *reinterpret_cast<const float4*>(sty + k);
+              const float4 Z = *reinterpret_cast<const float4*>(stz + k);
+              const f32x2 rx01 = f2_add(ox2, f2_pack(X.x, X.y)), rx23 = f2_add(ox2, f2_pack(X.z, X.w));
+              const f32x2 ry01 = f2_add(oy2, f2_pack(Y.x, Y.y)), ry23 = f2_add(oy2, f2_pack(Y.z, Y.w));
+              const f32x2 rz01 = f2_add(oz2, f2_pack(Z.x, Z.y)), rz23 = f2_add(oz2, f2_pack(Z.z, Z.w));
+              const f32x2 q01 = f2_fma(rx01, rx01, f2_fma(ry01, ry01, f2_mul(rz01, rz01)));
+              const f32x2 q23 = f2_fma(rx23, rx23, f2_fma(ry23, ry23, f2_mul(rz23, rz23)));
+              float r0, r1, r2, r3;
+              f2_unpack(q01, r0, r1);
+              f2_unpack(q23, r2, r3);
+              const unsigned nib = (r0 < rl2 ? 1u : 0u) | (r1 < rl2 ? 2u : 0u) | (r2 < rl2 ? 4u : 0u) |
+                                   (r3 < rl2 ? 8u : 0u);
+              hits |= nib << k;
+            }
+#elif GBMD_LIST_UNROLL4
             for (int k = 0; k < m; k += 4) {
               unsigned nib = 0u;
 #pragma unroll

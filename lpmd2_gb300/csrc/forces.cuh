@@ -310,6 +310,15 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_tail(Dev D, int count_step, in
 #ifndef GBMD_FORCE_MIN_BLOCKS
 #define GBMD_FORCE_MIN_BLOCKS 8
 #endif
+// The same for the mixed EAM density pass (0: no minimum, the compiler's own choice).
+#ifndef GBMD_DENSITY_MIN_BLOCKS
+#define GBMD_DENSITY_MIN_BLOCKS 0
+#endif
+#if GBMD_DENSITY_MIN_BLOCKS > 0
+#define GBMD_DENSITY_BOUNDS __launch_bounds__(TILE, GBMD_DENSITY_MIN_BLOCKS)
+#else
+#define GBMD_DENSITY_BOUNDS __launch_bounds__(TILE)
+#endif
 
 // List groups per ring iteration of the pair force pass (1 or 2; the EAM force pass uses 1: two
 // groups spill its registers).
@@ -856,7 +865,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
 template <int SCM>
-__global__ void __launch_bounds__(TILE) k_eam_density32(Dev D, PotParams P) {
+__global__ void GBMD_DENSITY_BOUNDS k_eam_density32(Dev D, PotParams P) {
   __shared__ float4 shifts[125];
   __shared__ __align__(16) uint4 ring_s[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar_s[TILE / 32][RING];

@@ -93,6 +93,15 @@ __global__ void __launch_bounds__(DECIDE_THREADS) k_decide(Dev D, int nsys, int 
 // Binning and counting sort
 // ---------------------------------------------------------------------------------------------
 
+// Sort-chain options: warp-aggregated cell atomics in k_bin / k_scatter (one atomic per cell
+// and warp instead of one per atom), several cells per thread in k_scan.
+#ifndef GBMD_SORT_AGGREGATE
+#define GBMD_SORT_AGGREGATE 1
+#endif
+#ifndef GBMD_SCAN_CELLS
+#define GBMD_SCAN_CELLS 4
+#endif
+
 __global__ void k_bin(Dev D) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N) return;
@@ -118,23 +127,38 @@ __global__ void k_bin(Dev D) {
   }
   int c = S.cell_base + (cz * S.n[1] + cy) * S.n[0] + cx;
   D.acell[i] = c;
+#if GBMD_SORT_AGGREGATE
+  // consecutive atoms mostly share a cell (the arrays are in the previous cell order): one
+  // atomic per cell and warp
+  const unsigned peers = __match_any_sync(__activemask(), c);
+  if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&D.ccount[c], __popc(peers));
+#else
   atomicAdd(&D.ccount[c], 1);
+#endif
 }
 
-// One block per system: exclusive scan of the cell counts; resets counts and cursors.
+// One block per system: exclusive scan of the cell counts, GBMD_SCAN_CELLS consecutive cells
+// per thread; resets counts and cursors.
 __global__ void k_scan(Dev D) {
   const int s = blockIdx.x;
   if (!D.sst[s].need_rebuild) return;
   const SysDev& S = D.sysd[s];
+  const int nc = S.ncells, cb = S.cell_base;
   __shared__ int warp_tot[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int base = 0; base < S.ncells; base += blockDim.x) {
-    int c = base + threadIdx.x;
-    int v = (c < S.ncells) ? D.ccount[S.cell_base + c] : 0;
-    int x = v;
+  for (int base = 0; base < nc; base += blockDim.x * GBMD_SCAN_CELLS) {
+    const int c0 = base + threadIdx.x * GBMD_SCAN_CELLS;
+    int v[GBMD_SCAN_CELLS];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < GBMD_SCAN_CELLS; ++k) {
+      v[k] = (c0 + k < nc) ? D.ccount[cb + c0 + k] : 0;
+      sum += v[k];
+    }
+    int x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -152,15 +176,19 @@ __global__ void k_scan(Dev D) {
       if (lane < nw) warp_tot[lane] = t;
     }
     __syncthreads();
-    int excl = x - v + (w > 0 ? warp_tot[w - 1] : 0) + carry;
-    if (c < S.ncells) {
-      D.cstart[S.cell_base + c] = (int)(S.atom_base) + excl;  // global slot
-      D.ccnt[S.cell_base + c] = v;
-      D.ccount[S.cell_base + c] = 0;
-      D.ccursor[S.cell_base + c] = 0;
+    int excl = x - sum + (w > 0 ? warp_tot[w - 1] : 0) + carry;
+#pragma unroll
+    for (int k = 0; k < GBMD_SCAN_CELLS; ++k) {
+      if (c0 + k < nc) {
+        D.cstart[cb + c0 + k] = (int)(S.atom_base) + excl;  // global slot
+        D.ccnt[cb + c0 + k] = v[k];
+        D.ccount[cb + c0 + k] = 0;
+        D.ccursor[cb + c0 + k] = 0;
+      }
+      excl += v[k];
     }
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    if (threadIdx.x == blockDim.x - 1) carry = excl;  // the block's running total
     __syncthreads();
   }
 }
@@ -185,7 +213,18 @@ __global__ void k_scatter(Dev D) {
   int s = D.sysid[i];
   if (!D.sst[s].need_rebuild) return;
   int c = D.acell[i];
+#if GBMD_SORT_AGGREGATE
+  // the warp's atoms of one cell take consecutive slots from one atomic (their order inside
+  // the cell is set by k_cellsort either way)
+  const unsigned peers = __match_any_sync(__activemask(), c);
+  const int lane = threadIdx.x & 31, lead = __ffs(peers) - 1;
+  int first = 0;
+  if (lane == lead) first = atomicAdd(&D.ccursor[c], __popc(peers));
+  first = __shfl_sync(peers, first, lead);
+  int p = D.cstart[c] + first + __popc(peers & ((1u << lane) - 1u));
+#else
   int p = D.cstart[c] + atomicAdd(&D.ccursor[c], 1);
+#endif
   D.perm[p] = (int)i;
 }
 

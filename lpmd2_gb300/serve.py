@@ -69,10 +69,17 @@ def footprint(systems: list[dict], rl: float) -> int:
 class Server:
     def __init__(self, backend, budget_bytes: float = 150e9, max_batches: int = 4, max_systems: int = 512,
                  chunk_steps: int = 5000, window_s: float = 0.2, fill_atoms: int = 2_000_000,
-                 small_atoms: int = 0, clock: Callable[[], float] = time.monotonic):
+                 small_atoms: int = 0, order: str = "arrival", max_batch_atoms: int = 0,
+                 clock: Callable[[], float] = time.monotonic):
         """window_s / fill_atoms: a batch is formed once its oldest waiting job has waited
         window_s, or once fill_atoms atoms of its class are waiting (enough to fill the GPU),
         so that jobs arriving close together share a batch instead of each taking a slot.
+
+        order: the order in which the waiting jobs of the chosen class go into a new batch:
+        "arrival", or "work" (least atoms x steps first).  max_batch_atoms: atoms one batch
+        takes at most (0: no limit; a single larger job still gets a batch of its own).  A batch
+        holds its slot until its longest job is done, so with "work" and a limit, batches of
+        short jobs turn their slots over quickly and a backlog is served shortest first.
 
         small_atoms: jobs below this size form their own batches (0: off, the default).  A
         batch steps in lockstep, so a small job with many steps sharing a batch with large
@@ -81,6 +88,10 @@ class Server:
         still wait for SM slots behind the large batches' running blocks."""
         self.backend = backend
         self.small_atoms = int(small_atoms)
+        if order not in ("arrival", "work"):
+            raise ValueError(f"unknown admission order {order!r}")
+        self.order = order
+        self.max_batch_atoms = int(max_batch_atoms)
         self.window_s = float(window_s)
         self.fill_atoms = int(fill_atoms)
         self.budget = float(budget_bytes)
@@ -155,12 +166,20 @@ class Server:
             kind = cls[0]
             rl = self.backend.list_radius(kind)
             picked: list[tuple[dict, dict]] = []
-            for job, system in waiting:
-                if self._class(job, system) != cls or len(picked) >= self.max_systems:
+            candidates = [(j, s) for j, s in waiting if self._class(j, s) == cls]
+            if self.order == "work":
+                candidates.sort(key=lambda js: (int(js[1]["natoms"]) * int(js[0]["steps"]), js[0]["arrival"]))
+            atoms = 0
+            for job, system in candidates:
+                if len(picked) >= self.max_systems:
+                    break
+                n = int(system["natoms"])
+                if self.max_batch_atoms and picked and atoms + n > self.max_batch_atoms:
                     continue
                 trial = [s for _, s in picked] + [system]
                 if self.used + footprint(trial, rl) <= self.budget:
                     picked.append((job, system))
+                    atoms += n
             if not picked:
                 return  # the oldest kind does not fit yet: wait for memory
             for p in picked:

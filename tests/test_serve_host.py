@@ -160,3 +160,32 @@ def test_lanes_follow_the_live_atoms():
 
     assert [lanes_for(n) for n in (500, 999, 1_000, 9_999, 10_000, 59_999, 60_000, 3_000_000)] == \
         [16, 16, 4, 4, 2, 2, 1, 1]
+
+
+def test_work_order_admits_shortest_first_within_the_atom_limit():
+    """order="work" with max_batch_atoms: every batch holds at most the limit (or one larger
+    job alone), all jobs still run their own steps, and a backlog is admitted shortest first:
+    the job with the least atoms x steps goes into the first batch, and the first batch's jobs
+    are shorter on average than the last batch's."""
+    jobs = [dict(j, arrival=0.0) for j in small_jobs(40, 50.0)]  # one backlog at t = 0
+    be = CountingBackend()
+    srv = Server(be, budget_bytes=150e9, max_batches=1, max_systems=64, order="work", max_batch_atoms=40000)
+    results = srv.serve(jobs, fake_system)
+    check_results(jobs, results, be, srv)
+    work = {}
+    atoms = {}
+    for j, r in zip(jobs, results):
+        work.setdefault(r.batch, []).append(4 * j["k"] ** 3 * j["steps"])
+        atoms.setdefault(r.batch, []).append(4 * j["k"] ** 3)
+    for b in atoms:
+        assert sum(atoms[b]) <= 40000 or len(atoms[b]) == 1
+    order = sorted(work)  # batch ids are given in admission order
+    assert len(order) > 2
+    least = min(4 * j["k"] ** 3 * j["steps"] for j in jobs)
+    assert least in work[order[0]]
+    assert np.mean(work[order[0]]) < np.mean(work[order[-1]])
+
+
+def test_unknown_admission_order_is_rejected():
+    with pytest.raises(ValueError, match="admission order"):
+        Server(CountingBackend(), order="random")

@@ -76,7 +76,8 @@ class Server:
         so that jobs arriving close together share a batch instead of each taking a slot.
 
         order: the order in which the waiting jobs of the chosen class go into a new batch:
-        "arrival", or "work" (least atoms x steps first).  max_batch_atoms: atoms one batch
+        "arrival", "work" (least atoms x steps first) or "steps" (fewest steps first, so that a
+        batch's jobs end close together).  max_batch_atoms: atoms one batch
         takes at most (0: no limit; a single larger job still gets a batch of its own).  A batch
         holds its slot until its longest job is done, so with "work" and a limit, batches of
         short jobs turn their slots over quickly and a backlog is served shortest first.
@@ -88,7 +89,7 @@ class Server:
         still wait for SM slots behind the large batches' running blocks."""
         self.backend = backend
         self.small_atoms = int(small_atoms)
-        if order not in ("arrival", "work"):
+        if order not in ("arrival", "work", "steps"):
             raise ValueError(f"unknown admission order {order!r}")
         self.order = order
         self.max_batch_atoms = int(max_batch_atoms)
@@ -169,6 +170,8 @@ class Server:
             candidates = [(j, s) for j, s in waiting if self._class(j, s) == cls]
             if self.order == "work":
                 candidates.sort(key=lambda js: (int(js[1]["natoms"]) * int(js[0]["steps"]), js[0]["arrival"]))
+            elif self.order == "steps":
+                candidates.sort(key=lambda js: (int(js[0]["steps"]), int(js[1]["natoms"]), js[0]["arrival"]))
             atoms = 0
             for job, system in candidates:
                 if len(picked) >= self.max_systems:

@@ -444,30 +444,31 @@ struct ShiftCorr {
 __device__ __forceinline__ ShiftCorr shift_corr(const SysDev& S) {
   return ShiftCorr{S.dfc[0], S.dfc[1], S.dfc[2]};
 }
+template <bool PACKED = (GBMD_F32X2 != 0)>
 __device__ __forceinline__ float entry_r2(const float4& gi, const float4& gj, const float4& sh, const ShiftCorr& c,
                                           float& dx, float& dy, float& dz) {
-#if GBMD_F32X2
-  // x and y as one packed pair (each float4's x, y sit in an aligned register pair)
-  const f32x2 shxy = f2_pack(sh.x, sh.y);
-  f32x2 dxy = f2_sub(f2_add(shxy, f2_pack(gj.x, gj.y)), f2_pack(gi.x, gi.y));
+  if constexpr (PACKED) {
+    // x and y as one packed pair (each float4's x, y sit in an aligned register pair)
+    const f32x2 shxy = f2_pack(sh.x, sh.y);
+    f32x2 dxy = f2_sub(f2_add(shxy, f2_pack(gj.x, gj.y)), f2_pack(gi.x, gi.y));
 #if GBMD_SHIFT_CORR
-  dxy = f2_fma(shxy, f2_pack(c.x, c.y), dxy);
+    dxy = f2_fma(shxy, f2_pack(c.x, c.y), dxy);
 #endif
-  f2_unpack(dxy, dx, dy);
-  dz = (sh.z + gj.z) - gi.z;
+    f2_unpack(dxy, dx, dy);
+    dz = (sh.z + gj.z) - gi.z;
 #if GBMD_SHIFT_CORR
-  dz = fmaf(sh.z, c.z, dz);
+    dz = fmaf(sh.z, c.z, dz);
 #endif
-#else
-  dx = (sh.x + gj.x) - gi.x;
-  dy = (sh.y + gj.y) - gi.y;
-  dz = (sh.z + gj.z) - gi.z;
+  } else {
+    dx = (sh.x + gj.x) - gi.x;
+    dy = (sh.y + gj.y) - gi.y;
+    dz = (sh.z + gj.z) - gi.z;
 #if GBMD_SHIFT_CORR
-  dx = fmaf(sh.x, c.x, dx);
-  dy = fmaf(sh.y, c.y, dy);
-  dz = fmaf(sh.z, c.z, dz);
+    dx = fmaf(sh.x, c.x, dx);
+    dy = fmaf(sh.y, c.y, dy);
+    dz = fmaf(sh.z, c.z, dz);
 #endif
-#endif
+  }
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 

@@ -310,6 +310,12 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_tail(Dev D, int count_step, in
 #ifndef GBMD_FORCE_MIN_BLOCKS
 #define GBMD_FORCE_MIN_BLOCKS 8
 #endif
+// Packed displacement arithmetic in the EAM force pass as well (the pair force pass always
+// uses it when GBMD_F32X2 is on).
+#ifndef GBMD_F32X2_EAM_FORCE
+#define GBMD_F32X2_EAM_FORCE 1
+#endif
+
 // The same for the mixed EAM density pass (0: no minimum, the compiler's own choice).
 #ifndef GBMD_DENSITY_MIN_BLOCKS
 #define GBMD_DENSITY_MIN_BLOCKS 0
@@ -465,6 +471,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     // f[14] = the Sutton-Chen many-body prefactor in the folded form, else 1) where gathered
     const float phi_i = (PC == PC_EAM && active) ? (PHI_IN_W ? gsrc[li].w : D.phif[i]) : 0.f;
     constexpr bool FOLDED = PHI_IN_W && SCN > 0;
+    constexpr bool PACKED_R2 = GBMD_F32X2 && (PC == PC_PAIR || GBMD_F32X2_EAM_FORCE);
     const int na = S.natoms;
     const int cnt = active ? D.ncount[i] : 0;
     const int ng = (cnt + 3) >> 2;
@@ -481,7 +488,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     auto pair = [&](unsigned e, bool valid, float& dx, float& dy, float& dz) -> float {
       const int j = (int)(e & LOCAL_MASK);
       const float4 gj = gsrc[j];
-      const float r2 = entry_r2(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
+      const float r2 = entry_r2<PACKED_R2>(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
       bool in = valid && r2 < rc2_lo;
       if (valid && r2 >= rc2_lo && r2 < rc2_hi) {  // guard band: decided in FP64 after the loop
         if (band_e == NO_BAND)

@@ -315,6 +315,13 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_tail(Dev D, int count_step, in
 #ifndef GBMD_F32X2_EAM_FORCE
 #define GBMD_F32X2_EAM_FORCE 1
 #endif
+// Pair functions of two list entries at a time in packed pairs (LJ; folded Sutton-Chen).
+#ifndef GBMD_F32X2_PAIRMATH_LJ
+#define GBMD_F32X2_PAIRMATH_LJ 1
+#endif
+#ifndef GBMD_F32X2_PAIRMATH_EAM
+#define GBMD_F32X2_PAIRMATH_EAM 1
+#endif
 
 // The same for the mixed EAM density pass (0: no minimum, the compiler's own choice).
 #ifndef GBMD_DENSITY_MIN_BLOCKS
@@ -517,16 +524,74 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
       szz = fmaf(fz, dz, szz);
       return g;
     };
+    // The same two entries at a time, with the pair functions' products of variables as packed
+    // FP32 pairs (LJ and folded Sutton-Chen; bitwise the values of `pair`).
+    auto geom = [&](unsigned e, bool valid, float& dx, float& dy, float& dz, bool& in, float& qj) -> float {
+      const int j = (int)(e & LOCAL_MASK);
+      const float4 gj = gsrc[j];
+      const float r2 = entry_r2<PACKED_R2>(gi, gj, shifts[e >> CODE_SHIFT], corr, dx, dy, dz);
+      in = valid && r2 < rc2_lo;
+      if (valid && r2 >= rc2_lo && r2 < rc2_hi) {
+        if (band_e == NO_BAND)
+          band_e = e;
+        else
+          band_more = true;
+      }
+      if (SPECIES) in = in && applies_to(P.spc_sum, ti, __float_as_int(gj.w));
+      qj = gj.w;
+      return r2;
+    };
+    auto accum = [&](float g, float en, bool in, float r2, float dx, float dy, float dz) -> float {
+      g = in ? g : 0.0f;
+      ge += in ? en : 0.0f;
+      gv = fmaf(g, r2, gv);
+      const float fx = g * dx, fy = g * dy, fz = g * dz;
+      sxx = fmaf(fx, dx, sxx);
+      sxy = fmaf(fx, dy, sxy);
+      sxz = fmaf(fx, dz, sxz);
+      syy = fmaf(fy, dy, syy);
+      syz = fmaf(fy, dz, syz);
+      szz = fmaf(fz, dz, szz);
+      return g;
+    };
+    auto two = [&](unsigned ea, unsigned eb, bool va, bool vb, float& ax, float& ay, float& az, float& bx,
+                   float& by, float& bz, float& ga, float& gb) {
+      bool ina, inb;
+      float qa, qb;
+      const float r2a = geom(ea, va, ax, ay, az, ina, qa);
+      const float r2b = geom(eb, vb, bx, by, bz, inb, qb);
+      float sa, sb, ena, enb;
+      if constexpr (PC == PC_PAIR) {
+        lj_pair32_x2(P, rcp_approx(r2a), rcp_approx(r2b), sa, sb, ena, enb);
+      } else if constexpr (FOLDED) {
+        eam_sc_pair32_q_x2<SCN, SCM>(P, r2a, r2b, phi_i, qa, qb, sa, sb, ena, enb);
+      } else {
+        sa = sb = ena = enb = 0.0f;  // not reached: `two` serves the LJ and folded forms only
+      }
+      ga = accum(sa, ena, ina, r2a, ax, ay, az);
+      gb = accum(sb, enb, inb, r2b, bx, by, bz);
+    };
+    constexpr bool PAIRED =
+        GBMD_F32X2 && ((PC == PC_PAIR && GBMD_F32X2_PAIRMATH_LJ) || (FOLDED && GBMD_F32X2_PAIRMATH_EAM));
     // One group of four entries (rem = entries left in the atom's list from this group on).
     auto group = [&](const uint4& cur, int rem) {
       ge = 0.f;
       gv = 0.f;
       float ax, ay, az, bx, by, bz;
-      float g0 = pair(cur.x, true, ax, ay, az);
-      float g1 = pair(cur.y, rem > 1, bx, by, bz);
+      float g0, g1;
+      if constexpr (PAIRED) {
+        two(cur.x, cur.y, true, rem > 1, ax, ay, az, bx, by, bz, g0, g1);
+      } else {
+        g0 = pair(cur.x, true, ax, ay, az);
+        g1 = pair(cur.y, rem > 1, bx, by, bz);
+      }
       float gx = fmaf(g1, bx, g0 * ax), gy = fmaf(g1, by, g0 * ay), gz = fmaf(g1, bz, g0 * az);
-      g0 = pair(cur.z, rem > 2, ax, ay, az);
-      g1 = pair(cur.w, rem > 3, bx, by, bz);
+      if constexpr (PAIRED) {
+        two(cur.z, cur.w, rem > 2, rem > 3, ax, ay, az, bx, by, bz, g0, g1);
+      } else {
+        g0 = pair(cur.z, rem > 2, ax, ay, az);
+        g1 = pair(cur.w, rem > 3, bx, by, bz);
+      }
       gx = fmaf(g1, bx, fmaf(g0, ax, gx));
       gy = fmaf(g1, by, fmaf(g0, ay, gy));
       gz = fmaf(g1, bz, fmaf(g0, az, gz));

@@ -188,8 +188,25 @@ __device__ __forceinline__ void eam_pair64(const PotParams& P, double r, double 
 __device__ __forceinline__ void lj_pair32(const PotParams& P, float inv, float& g, float& e) {
   float x = fmaf(P.f[0], inv, P.f[4] * inv);  // one rounding of (f[0] + f[4]) * inv
   float r6 = x * x * x;
-  g = -inv * r6 * (P.f[1] * r6 - P.f[2]);
-  e = r6 * (P.f[3] * r6 - P.f[3]);
+  g = -inv * r6 * fmaf(P.f[1], r6, -P.f[2]);
+  e = r6 * fmaf(P.f[3], r6, -P.f[3]);
+}
+
+// lj_pair32 for two list entries, the products of variables as packed FP32 pairs and the
+// products with the parameters as scalars (their operands stay in the constant bank); every
+// value is bitwise the scalar form's.  The sign of g is carried by the bracket: (inv r6)
+// (f2 - f1 r6) = (-inv r6)(f1 r6 - f2) exactly, rounding being symmetric.
+__device__ __forceinline__ void lj_pair32_x2(const PotParams& P, float inva, float invb, float& ga, float& gb,
+                                             float& ea, float& eb) {
+  const float xa = fmaf(P.f[0], inva, P.f[4] * inva), xb = fmaf(P.f[0], invb, P.f[4] * invb);
+  const f32x2 x = f2_pack(xa, xb);
+  const f32x2 r6 = f2_mul(f2_mul(x, x), x);
+  float r6a, r6b;
+  f2_unpack(r6, r6a, r6b);
+  const f32x2 nt = f2_pack(fmaf(-P.f[1], r6a, P.f[2]), fmaf(-P.f[1], r6b, P.f[2]));
+  f2_unpack(f2_mul(f2_mul(f2_pack(inva, invb), r6), nt), ga, gb);
+  const f32x2 u = f2_pack(fmaf(P.f[3], r6a, -P.f[3]), fmaf(P.f[3], r6b, -P.f[3]));
+  f2_unpack(f2_mul(r6, u), ea, eb);
 }
 
 __device__ __forceinline__ float eam_rho32(const PotParams& P, float r2) {
@@ -296,6 +313,46 @@ __device__ __forceinline__ void eam_sc_pair32_q(const PotParams& P, float r2, fl
   const float pn = (N % 2 == 0) ? ipow_c<N / 2>(inv) : ipow_c<N / 2>(inv) * ir;  // r^-N
   e = P.f[0] * pn;
   s = fmaf(P.f[1], pn * inv, (qi + qj) * pm);
+}
+
+// x^N of a packed pair by the same repeated squaring as ipow_c.
+template <int N>
+__device__ __forceinline__ f32x2 ipow_c_x2(f32x2 x) {
+  if constexpr (N == 1) {
+    return x;
+  } else if constexpr (N % 2 == 0) {
+    const f32x2 h = ipow_c_x2<N / 2>(x);
+    return f2_mul(h, h);
+  } else {
+    return f2_mul(x, ipow_c_x2<N - 1>(x));
+  }
+}
+
+// eam_sc_pair32_q for two list entries (qja, qjb: the neighbours' factors), bitwise the same
+// values: the products of variables packed, the products with constants scalar.
+template <int N, int M>
+__device__ __forceinline__ void eam_sc_pair32_q_x2(const PotParams& P, float r2a, float r2b, float qi, float qja,
+                                                   float qjb, float& sa, float& sb, float& ea, float& eb) {
+  static_assert(M % 2 == 0 && M >= 2 && N >= 2, "the folded form takes even m");
+  // rsqrt_nr per lane: y = rsqrt(x); e = 1 - (x y) y; y + (y/2) e
+  const float ya = rsqrtf(r2a), yb = rsqrtf(r2b);
+  const f32x2 y = f2_pack(ya, yb);
+  float pa, pb;
+  f2_unpack(f2_mul(f2_pack(r2a, r2b), y), pa, pb);
+  const f32x2 e = f2_pack(fmaf(-pa, ya, 1.0f), fmaf(-pb, yb, 1.0f));
+  const f32x2 ir = f2_fma(f2_pack(0.5f * ya, 0.5f * yb), e, y);
+  const f32x2 inv = f2_mul(ir, ir);
+  const f32x2 pm = ipow_c_x2<(M + 2) / 2>(inv);                                            // r^-(M+2)
+  const f32x2 pn = (N % 2 == 0) ? ipow_c_x2<N / 2>(inv) : f2_mul(ipow_c_x2<N / 2>(inv), ir);  // r^-N
+  float pna, pnb;
+  f2_unpack(pn, pna, pnb);
+  ea = P.f[0] * pna;
+  eb = P.f[0] * pnb;
+  float pia, pib, qa, qb;
+  f2_unpack(f2_mul(pn, inv), pia, pib);
+  f2_unpack(f2_mul(f2_add(f2_pack(qi, qi), f2_pack(qja, qjb)), pm), qa, qb);
+  sa = fmaf(P.f[1], pia, qa);
+  sb = fmaf(P.f[1], pib, qb);
 }
 
 template <int N, int M>

@@ -333,8 +333,10 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_tail(Dev D, int count_step, in
 #define GBMD_DENSITY_BOUNDS __launch_bounds__(TILE)
 #endif
 
-// List groups per ring iteration of the pair force pass (1 or 2; the EAM force pass uses 1: two
-// groups spill its registers).
+// List groups per ring iteration of the pair and the EAM force passes (1 or 2).
+#ifndef GBMD_EAM_RING_GROUPS
+#define GBMD_EAM_RING_GROUPS 2
+#endif
 #ifndef GBMD_PAIR_RING_GROUPS
 #define GBMD_PAIR_RING_GROUPS 2
 #endif
@@ -608,7 +610,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
     bool waited = true;
-    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) {
+    if constexpr ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) || (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2)) {
       // two list groups per iteration: eight neighbour gathers in flight per lane
       waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], [&](int q, const uint4& cur) {
         if (q < ng) group(cur, cnt - 4 * q);

@@ -148,6 +148,10 @@ struct Dev {
   // multi-potential accumulation
   long long* facc;   // 3*N fixed point
   double* dacc;      // 3*N FP64
+  // SM-local tile claims of the mixed force and density passes: one counter per SM slot and a
+  // completion counter (claim_slots + 1 entries, zero between launches)
+  unsigned* tile_claim;
+  int claim_slots;
   // reductions
   double* tile_d;
   unsigned long long* sys_acc;  // nsys * SA_LEN

@@ -581,6 +581,12 @@ struct Engine::Impl {
     D.facc = alloc<long long>(3 * n);
     D.dacc = alloc<double>(3 * n);
     D.tile_d = alloc<double>((size_t)ntiles * PART_D);
+    {
+      int nsm = 0;
+      CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+      D.claim_slots = nsm > 0 ? nsm : 1;
+      D.tile_claim = alloc<unsigned>((size_t)D.claim_slots + 1);  // zeroed
+    }
     D.sys_acc = alloc<unsigned long long>((size_t)nsys * SA_LEN);
     D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
     D.log_cap = log_cap;

@@ -437,10 +437,57 @@ __device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, i
   return true;
 }
 
-template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
-__global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
+// Tile of a block of the mixed force and density passes: blockIdx.x, or with GBMD_SM_TILES=1 a
+// tile claimed from a contiguous range per SM (a block takes the next tile of the range of the
+// SM it runs on, of the next SM's once that range is used up), so that the blocks resident on an
+// SM at the same time work on neighbouring cells and share their neighbours' positions in L1.
+// Every block gets exactly one tile: a launch has as many blocks as tiles, each block claims at
+// most one, and a block that scanned every range without success would mean that the other
+// blocks had claimed all tiles.  The last block of a launch to finish zeroes the counters.
+// Measured on the GB300 (results bitwise equal): LJ force pass 150 us against 93 us with
+// blockIdx.x, copper density + force 0.590 against 0.480 ms, so the claim is off by default.
+#ifndef GBMD_SM_TILES
+#define GBMD_SM_TILES 0
+#endif
+__device__ __forceinline__ int claim_tile(const Dev& D) {
+#if GBMD_SM_TILES
+  __shared__ int s_tile;
+  if (threadIdx.x == 0) {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const int P = D.claim_slots, T = (int)gridDim.x;
+    int k = (int)(smid % (unsigned)P), tile = -1;
+    for (int probe = 0; probe < P && tile < 0; ++probe) {
+      const int lo = (int)((long long)T * k / P), n = (int)((long long)T * (k + 1) / P) - lo;
+      if (n > 0 && (int)__ldcg(D.tile_claim + k) < n) {
+        const int idx = (int)atomicAdd(D.tile_claim + k, 1u);
+        if (idx < n) tile = lo + idx;
+      }
+      k = (k + 1 == P) ? 0 : k + 1;
+    }
+    s_tile = tile;
+  }
+  __syncthreads();
+  return s_tile;
+#else
+  return (int)blockIdx.x;
+#endif
+}
+__device__ __forceinline__ void release_tile(const Dev& D) {
+#if GBMD_SM_TILES
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(D.tile_claim + D.claim_slots, 1u) == gridDim.x - 1) {
+      for (int k = 0; k <= D.claim_slots; ++k) D.tile_claim[k] = 0u;
+      __threadfence();
+    }
+  }
+#endif
+}
+
+template <int PC, int SPECIES, int SCN, int SCM>
+__device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, const StepParams& sp, const int tile) {
   __shared__ float4 shifts[125];
-  const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   if (!S.active) {  // whole block: one tile belongs to one system
@@ -743,6 +790,14 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, 
   }
 }
 
+
+template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
+__global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
+  const int tile = claim_tile(D);
+  if (tile >= 0) force32_tile<PC, SPECIES, SCN, SCM>(D, P, sp, tile);
+  release_tile(D);
+}
+
 // ------------------------------------------------------------------------------------------
 // Mixed LJ force pass with LANES lanes per atom (LANES = 2, 4, 8: 16, 8 or 4 atoms per warp),
 // for systems too small to fill the GPU one lane per atom.  The atom's list groups go
@@ -939,11 +994,10 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
 template <int SCM>
-__global__ void GBMD_DENSITY_BOUNDS k_eam_density32(Dev D, PotParams P) {
+__device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P, const int tile) {
   __shared__ float4 shifts[125];
   __shared__ __align__(16) uint4 ring_s[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar_s[TILE / 32][RING];
-  const int tile = blockIdx.x;
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   if (!S.active) return;  // whole block: one tile belongs to one system
@@ -1030,6 +1084,14 @@ __global__ void GBMD_DENSITY_BOUNDS k_eam_density32(Dev D, PotParams P) {
   long long t[1];
   block_sum<long long, 1>(v, t);
   if (threadIdx.x == 0) atomicAdd(D.sys_acc + (long long)s * SA_LEN + SA_EEMBED, (unsigned long long)t[0]);
+}
+
+
+template <int SCM>
+__global__ void GBMD_DENSITY_BOUNDS k_eam_density32(Dev D, PotParams P) {
+  const int tile = claim_tile(D);
+  if (tile >= 0) density32_tile<SCM>(D, P, tile);
+  release_tile(D);
 }
 
 // FP64 density pass (the plain path, any neighbour mode): reference r and rhoij, FP64

@@ -437,6 +437,42 @@ __device__ __forceinline__ bool warp_list_ring2(const Dev& D, const SysDev& S, i
   return true;
 }
 
+// Streaming 16-byte load that does not allocate in L1 (the list is read once per launch; L1 is
+// left to the neighbour gathers).
+__device__ __forceinline__ uint4 ld_stream(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+
+// As warp_list_ring2 with the list rows in registers instead of shared memory: each lane loads
+// its own 16-byte entry of rows q + 2 and q + 3 while rows q and q + 1 are evaluated.  Lanes
+// without an atom (has = false) load nothing; rows up to the warp's largest group count lie
+// inside every atom's list capacity.
+template <class F>
+__device__ __forceinline__ void warp_list_prefetch2(const Dev& D, const SysDev& S, int li, bool has, int ngw, F&& body) {
+  const uint4* src = list_group(D, S, li, 0);
+  const long long row = S.natoms;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  uint4 n0 = (has && ngw > 0) ? ld_stream(src) : zero;
+  uint4 n1 = (has && ngw > 1) ? ld_stream(src + row) : zero;
+  for (int q = 0; q < ngw; q += 2) {
+    const uint4 c0 = n0, c1 = n1;
+    if (has && q + 2 < ngw) n0 = ld_stream(src + (long long)(q + 2) * row);
+    if (has && q + 3 < ngw) n1 = ld_stream(src + (long long)(q + 3) * row);
+    body(q, c0);
+    if (q + 1 < ngw) body(q + 1, c1);
+  }
+}
+
+// List rows of the pair force pass through the bulk-copy ring in shared memory (1) or through
+// registers with L1-bypassing loads (0).
+#ifndef GBMD_PAIR_LIST_TMA
+#define GBMD_PAIR_LIST_TMA 1
+#endif
+
 // Tile of a block of the mixed force and density passes: blockIdx.x, or with GBMD_SM_TILES=1 a
 // tile claimed from a contiguous range per SM (a block takes the next tile of the range of the
 // SM it runs on, of the next SM's once that range is used up), so that the blocks resident on an
@@ -657,7 +693,11 @@ __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, c
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
     bool waited = true;
-    if constexpr ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) || (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2)) {
+    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2 && !GBMD_PAIR_LIST_TMA) {
+      warp_list_prefetch2(D, S, li, lane < wcount, ngw, [&](int q, const uint4& cur) {
+        if (q < ng) group(cur, cnt - 4 * q);
+      });
+    } else if constexpr ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) || (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2)) {
       // two list groups per iteration: eight neighbour gathers in flight per lane
       waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring[w], bar[w], [&](int q, const uint4& cur) {
         if (q < ng) group(cur, cnt - 4 * q);

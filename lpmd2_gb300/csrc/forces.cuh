@@ -467,10 +467,16 @@ __device__ __forceinline__ void warp_list_prefetch2(const Dev& D, const SysDev& 
   }
 }
 
-// List rows of the pair force pass through the bulk-copy ring in shared memory (1) or through
-// registers with L1-bypassing loads (0).
+// List rows of the pair force pass (of the EAM force and density passes) through the bulk-copy
+// ring in shared memory (1) or through registers with L1-bypassing loads (0).  Measured on the
+// GB300 with results bitwise equal: the register form is 1.8 % faster on the LJ force pass and
+// 1.6 % on the copper passes -- without the ring's shared memory the L1 that serves the
+// neighbour gathers is 32 KB larger per SM (a 32 KB instead of a 64 KB shared-memory carve-out).
 #ifndef GBMD_PAIR_LIST_TMA
-#define GBMD_PAIR_LIST_TMA 1
+#define GBMD_PAIR_LIST_TMA 0
+#endif
+#ifndef GBMD_EAM_LIST_TMA
+#define GBMD_EAM_LIST_TMA 0
 #endif
 
 // Tile of a block of the mixed force and density passes: blockIdx.x, or with GBMD_SM_TILES=1 a
@@ -693,7 +699,8 @@ __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, c
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
     bool waited = true;
-    if constexpr (PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2 && !GBMD_PAIR_LIST_TMA) {
+    if constexpr ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2 && !GBMD_PAIR_LIST_TMA) ||
+                  (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2 && !GBMD_EAM_LIST_TMA)) {
       warp_list_prefetch2(D, S, li, lane < wcount, ngw, [&](int q, const uint4& cur) {
         if (q < ng) group(cur, cnt - 4 * q);
       });
@@ -1077,13 +1084,18 @@ __device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P,
   const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
   const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
   const int ngw = __reduce_max_sync(0xffffffffu, (unsigned)ng);
-  const bool waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], [&](int g, const uint4& e4) {
+  auto row = [&](int g, const uint4& e4) {
     if (g < ng) {
       const int rem = cnt - 4 * g;
       const float part = ((term(e4.x, true) + term(e4.y, rem > 1)) + term(e4.z, rem > 2)) + term(e4.w, rem > 3);
       q.add(part * scale);
     }
-  });
+  };
+  bool waited = true;
+  if constexpr (GBMD_EAM_LIST_TMA)
+    waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], row);
+  else
+    warp_list_prefetch2(D, S, li, active, ngw, row);
   if (!waited) atomicOr(&D.sst[s].error, ERR_WAIT);
   if (band_e != NO_BAND) {
     auto settle = [&](unsigned e) {

@@ -280,6 +280,7 @@ struct Engine::Impl {
   int graph_block = 10;
   int graph_mode = 2;  // 0 direct, 1 captured, 2 captured with conditional rebuild
   int lanes = 1;       // lanes per atom of the mixed LJ force pass
+  int list_feed = 0;   // list rows of the mixed passes: 0 auto (ring for batches), 1 registers, 2 ring
   int stencil_r = 1;
   int log_cap = 1024;
 
@@ -912,12 +913,17 @@ struct Engine::Impl {
       const bool sc126 = P.kind == POT_SC && P.int_n == 12 && P.int_m == 6;
       PotParams Pe = P;
       Pe.f[14] = (!species && (sc96 || sc126)) ? P.f[2] : 1.0f;  // scale of the density pass's copy
+      // list rows through registers for a single system, through the shared-memory ring for
+      // ensembles (the faster of the two on the GB300 for each), unless the option says otherwise
+      const bool ring = list_feed == 2 || (list_feed == 0 && nsys > 1);
       if (!pair_kind(P.kind)) {
         int first = (p == first_eam);
         if (mixed && P.kind == POT_SC && P.int_m == 6)
-          k_eam_density32<6><<<ntiles, TILE, 0, s>>>(D, Pe);
+          ring ? k_eam_density32<6, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe)
+               : k_eam_density32<6, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe);
         else if (mixed)
-          k_eam_density32<0><<<ntiles, TILE, 0, s>>>(D, Pe);
+          ring ? k_eam_density32<0, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe)
+               : k_eam_density32<0, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe);
         else if (mode == NB_LIST)
           k_eam_density<NB_LIST><<<ntiles, TILE, 0, s>>>(D, P, first);
         else if (mode == NB_CELLS)
@@ -941,18 +947,24 @@ struct Engine::Impl {
             species ? k_force32_lanes<1, 32><<<g, TILE, 0, s>>>(D, P, sp) : k_force32_lanes<0, 32><<<g, TILE, 0, s>>>(D, P, sp);
         } else if (pair_kind(P.kind)) {
           if (species)
-            k_force32<PC_PAIR, 1><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            ring ? k_force32<PC_PAIR, 1, 0, 0, FEED_RING><<<ntiles, TILE, 0, s>>>(D, P, sp)
+                 : k_force32<PC_PAIR, 1, 0, 0, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, P, sp);
           else
-            k_force32<PC_PAIR, 0><<<ntiles, TILE, 0, s>>>(D, P, sp);
+            ring ? k_force32<PC_PAIR, 0, 0, 0, FEED_RING><<<ntiles, TILE, 0, s>>>(D, P, sp)
+                 : k_force32<PC_PAIR, 0, 0, 0, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, P, sp);
         } else {
           if (species)
-            k_force32<PC_EAM, 1><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
+            ring ? k_force32<PC_EAM, 1, 0, 0, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe, sp)
+                 : k_force32<PC_EAM, 1, 0, 0, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else if (sc96)
-            k_force32<PC_EAM, 0, 9, 6><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
+            ring ? k_force32<PC_EAM, 0, 9, 6, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe, sp)
+                 : k_force32<PC_EAM, 0, 9, 6, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else if (sc126)
-            k_force32<PC_EAM, 0, 12, 6><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
+            ring ? k_force32<PC_EAM, 0, 12, 6, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe, sp)
+                 : k_force32<PC_EAM, 0, 12, 6, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
           else
-            k_force32<PC_EAM, 0><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
+            ring ? k_force32<PC_EAM, 0, 0, 0, FEED_RING><<<ntiles, TILE, 0, s>>>(D, Pe, sp)
+                 : k_force32<PC_EAM, 0, 0, 0, FEED_REGS><<<ntiles, TILE, 0, s>>>(D, Pe, sp);
         }
       } else if (mode == NB_LIST) {
         if (pair_kind(P.kind))
@@ -1585,7 +1597,14 @@ void Engine::set_option(const std::string& key, const std::string& value) {
     I.set_priority(v != 0.0 ? 1 : 0);
     return;
   }
-  if (key == "lanes_per_atom") {  // mixed LJ force pass: 1 (bulk-copy ring), 2, 4, 8, 16 or 32 lanes per atom
+  if (key == "list_feed") {  // list rows of the mixed passes: 0 auto, 1 registers, 2 shared-memory ring
+    const int f = (int)v;
+    if (f < 0 || f > 2) throw Error(1, "list_feed must be 0 (auto), 1 (registers) or 2 (ring)");
+    I.list_feed = f;
+    I.drop_graph();
+    return;
+  }
+  if (key == "lanes_per_atom") {  // mixed LJ force pass: 1 (one lane per atom), 2, 4, 8, 16 or 32 lanes per atom
     const int l = (int)v;
     if (l != 1 && l != 2 && l != 4 && l != 8 && l != 16 && l != 32)
       throw Error(1, "lanes_per_atom must be 1, 2, 4, 8, 16 or 32");

@@ -467,17 +467,13 @@ __device__ __forceinline__ void warp_list_prefetch2(const Dev& D, const SysDev& 
   }
 }
 
-// List rows of the pair force pass (of the EAM force and density passes) through the bulk-copy
-// ring in shared memory (1) or through registers with L1-bypassing loads (0).  Measured on the
-// GB300 with results bitwise equal: the register form is 1.8 % faster on the LJ force pass and
-// 1.6 % on the copper passes -- without the ring's shared memory the L1 that serves the
-// neighbour gathers is 32 KB larger per SM (a 32 KB instead of a 64 KB shared-memory carve-out).
-#ifndef GBMD_PAIR_LIST_TMA
-#define GBMD_PAIR_LIST_TMA 0
-#endif
-#ifndef GBMD_EAM_LIST_TMA
-#define GBMD_EAM_LIST_TMA 0
-#endif
+// How the mixed force and density passes read their list rows (template parameter FEED, chosen
+// per launch): FEED_REGS, each lane loads its own entries into registers with L1-bypassing loads;
+// FEED_RING, bulk asynchronous copies into a per-warp shared-memory ring.  Results are bitwise
+// the same.  Measured on the GB300: single large systems run 1.6-1.8 % faster with registers
+// (without the ring's shared memory the L1 that serves the neighbour gathers is 32 KB larger
+// per SM), the 512-system LJ ensemble 2.6 % faster with the ring.
+constexpr int FEED_REGS = 0, FEED_RING = 1;
 
 // Tile of a block of the mixed force and density passes: blockIdx.x, or with GBMD_SM_TILES=1 a
 // tile claimed from a contiguous range per SM (a block takes the next tile of the range of the
@@ -527,7 +523,7 @@ __device__ __forceinline__ void release_tile(const Dev& D) {
 #endif
 }
 
-template <int PC, int SPECIES, int SCN, int SCM>
+template <int PC, int SPECIES, int SCN, int SCM, int FEED>
 __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, const StepParams& sp, const int tile) {
   __shared__ float4 shifts[125];
   const int s = D.tile_sys[tile];
@@ -699,8 +695,8 @@ __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, c
     const int wfirst = D.tile_first[tile] - (int)S.atom_base + 32 * w;
     const int wcount = min(32, max(0, D.tile_count[tile] - 32 * w));
     bool waited = true;
-    if constexpr ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2 && !GBMD_PAIR_LIST_TMA) ||
-                  (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2 && !GBMD_EAM_LIST_TMA)) {
+    if constexpr (FEED == FEED_REGS &&
+                  ((PC == PC_PAIR && GBMD_PAIR_RING_GROUPS == 2) || (PC == PC_EAM && GBMD_EAM_RING_GROUPS == 2))) {
       warp_list_prefetch2(D, S, li, lane < wcount, ngw, [&](int q, const uint4& cur) {
         if (q < ng) group(cur, cnt - 4 * q);
       });
@@ -838,10 +834,10 @@ __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, c
 }
 
 
-template <int PC, int SPECIES, int SCN = 0, int SCM = 0>
+template <int PC, int SPECIES, int SCN = 0, int SCM = 0, int FEED = FEED_REGS>
 __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32(Dev D, PotParams P, StepParams sp) {
   const int tile = claim_tile(D);
-  if (tile >= 0) force32_tile<PC, SPECIES, SCN, SCM>(D, P, sp, tile);
+  if (tile >= 0) force32_tile<PC, SPECIES, SCN, SCM, FEED>(D, P, sp, tile);
   release_tile(D);
 }
 
@@ -1040,7 +1036,7 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
 // Mixed density pass over the Verlet list: FP32 rho_ij of each group of four entries
 // (branch-free, out-of-range entries masked), the group sum added to the int64 fixed-point
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
-template <int SCM>
+template <int SCM, int FEED>
 __device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P, const int tile) {
   __shared__ float4 shifts[125];
   __shared__ __align__(16) uint4 ring_s[TILE / 32][RING][32];
@@ -1092,7 +1088,7 @@ __device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P,
     }
   };
   bool waited = true;
-  if constexpr (GBMD_EAM_LIST_TMA)
+  if constexpr (FEED == FEED_RING)
     waited = warp_list_ring2(D, S, wfirst, wcount, ngw, ring_s[w], bar_s[w], row);
   else
     warp_list_prefetch2(D, S, li, active, ngw, row);
@@ -1139,10 +1135,10 @@ __device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P,
 }
 
 
-template <int SCM>
+template <int SCM, int FEED = FEED_REGS>
 __global__ void GBMD_DENSITY_BOUNDS k_eam_density32(Dev D, PotParams P) {
   const int tile = claim_tile(D);
-  if (tile >= 0) density32_tile<SCM>(D, P, tile);
+  if (tile >= 0) density32_tile<SCM, FEED>(D, P, tile);
   release_tile(D);
 }
 

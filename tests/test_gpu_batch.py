@@ -149,3 +149,27 @@ def test_lanes_per_atom_give_the_same_trajectory(lanes):
         assert x["potential_energy"] == y["potential_energy"]
         assert x["virial"] == y["virial"]
         np.testing.assert_allclose(x["stress"], y["stress"], rtol=1e-6, atol=1e-9 * np.abs(y["stress"]).max())
+
+
+@pytest.mark.parametrize("kind", ["lj", "sc"])
+def test_list_feeds_agree_bitwise(kind):
+    """The mixed passes read their list rows through registers (list_feed 1, the default for a
+    single system) or through the shared-memory ring of bulk copies (list_feed 2, the default
+    for a batch).  Both feed the same entries to the same arithmetic: a batch run with either
+    ends bit for bit the same."""
+    systems = lj_systems()[:3] if kind == "lj" else sc_systems()[:2]
+    runs = []
+    for feed in (1, 2):
+        b = gbmd.Batch([s["natoms"] for s in systems], [s["L"] for s in systems])
+        for k, s in enumerate(systems):
+            b.set_atoms(k, s["pos"], s["vel"], Z=s["Z"], mass=s["mass"])
+        setup(b, kind, "mixed")
+        b.set_option("list_feed", feed)
+        b.update_forces()
+        b.do_steps(30)
+        runs.append([(b.atoms(k), b.thermo(k)["raw"]) for k in range(len(systems))])
+        b.close()
+    for (a1, t1), (a2, t2) in zip(runs[0], runs[1]):
+        for x, y in zip(a1, a2):
+            np.testing.assert_array_equal(x, y)
+        np.testing.assert_array_equal(t1, t2)

@@ -183,8 +183,8 @@ gbmd_status gbmd_sim_set_precision(gbmd_sim* sim, int precision);
  *                      share an atom's neighbour list, i.e. 32 to 1 atoms per warp (same
  *                      forces bit for bit; for small systems)
  *   "list_feed"        how the mixed passes read their Verlet-list rows: 0 auto (default:
- *                      registers for a single system, a shared-memory ring of bulk copies for
- *                      a batch), 1 registers, 2 ring (the same results either way) */
+ *                      registers for a single EAM system, a shared-memory ring of bulk copies
+ *                      otherwise), 1 registers, 2 ring (the same results either way) */
 gbmd_status gbmd_sim_set_option(gbmd_sim* sim, const char* key, const char* value);
 
 /* CombinedPotential::UpdateForces (liblpmd/lpmd/combinedpotential.h:39-52): zeroes

@@ -152,6 +152,9 @@ struct Dev {
   // completion counter (claim_slots + 1 entries, zero between launches)
   unsigned* tile_claim;
   int claim_slots;
+  // per-system cell-shift tables (128 float4 per system, entries 0..124 used) for the mixed
+  // passes that read them from global memory instead of shared memory (GBMD_SHIFTS_GLOBAL)
+  float4* shift_tab;
   // reductions
   double* tile_d;
   unsigned long long* sys_acc;  // nsys * SA_LEN

@@ -280,7 +280,7 @@ struct Engine::Impl {
   int graph_block = 10;
   int graph_mode = 2;  // 0 direct, 1 captured, 2 captured with conditional rebuild
   int lanes = 1;       // lanes per atom of the mixed LJ force pass
-  int list_feed = 0;   // list rows of the mixed passes: 0 auto (ring for batches), 1 registers, 2 ring
+  int list_feed = 0;   // list rows of the mixed passes: 0 auto, 1 registers, 2 ring
   int stencil_r = 1;
   int log_cap = 1024;
 
@@ -588,6 +588,7 @@ struct Engine::Impl {
       D.claim_slots = nsm > 0 ? nsm : 1;
       D.tile_claim = alloc<unsigned>((size_t)D.claim_slots + 1);  // zeroed
     }
+    D.shift_tab = alloc<float4>((size_t)nsys * 128);
     D.sys_acc = alloc<unsigned long long>((size_t)nsys * SA_LEN);
     D.thermo_last = alloc<double>((size_t)nsys * THERMO_LEN);
     D.log_cap = log_cap;
@@ -642,7 +643,21 @@ struct Engine::Impl {
 
   void upload_sysd() {
     CK(cudaMemcpyAsync(d_sysd, sysd.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, stream));
+    if (D.shift_tab) {
+      // k * (FP32 cell edge) per axis, k in -2..2, as load_shifts computes it on the device
+      // (a product with 0, +-1 or +-2 is exact, so host and device agree bit for bit)
+      shift_host.assign((size_t)nsys * 128, make_float4(0.f, 0.f, 0.f, 0.f));
+      for (int s = 0; s < nsys; ++s)
+        for (int c = 0; c < 125; ++c) {
+          const int kx = c % 5 - 2, ky = (c / 5) % 5 - 2, kz = c / 25 - 2;
+          shift_host[(size_t)s * 128 + c] = make_float4((float)kx * sysd[s].df[0], (float)ky * sysd[s].df[1],
+                                                        (float)kz * sysd[s].df[2], 0.0f);
+        }
+      CK(cudaMemcpyAsync(D.shift_tab, shift_host.data(), sizeof(float4) * shift_host.size(), cudaMemcpyHostToDevice,
+                         stream));
+    }
   }
+  std::vector<float4> shift_host;  // pageable: the copy has taken the data when it returns
 
   ~Impl() {
     if (device >= 0) cudaSetDevice(device);
@@ -913,9 +928,10 @@ struct Engine::Impl {
       const bool sc126 = P.kind == POT_SC && P.int_n == 12 && P.int_m == 6;
       PotParams Pe = P;
       Pe.f[14] = (!species && (sc96 || sc126)) ? P.f[2] : 1.0f;  // scale of the density pass's copy
-      // list rows through registers for a single system, through the shared-memory ring for
-      // ensembles (the faster of the two on the GB300 for each), unless the option says otherwise
-      const bool ring = list_feed == 2 || (list_feed == 0 && nsys > 1);
+      // list rows through the shared-memory ring for ensembles and pair potentials, through
+      // registers for a single EAM system (the faster of the two on the GB300 for each), unless
+      // the option says otherwise
+      const bool ring = list_feed == 2 || (list_feed == 0 && (nsys > 1 || pair_kind(P.kind)));
       if (!pair_kind(P.kind)) {
         int first = (p == first_eam);
         if (mixed && P.kind == POT_SC && P.int_m == 6)

@@ -70,6 +70,20 @@ __device__ __forceinline__ void load_shifts(const SysDev& S, float4* sh) {
   __syncthreads();
 }
 
+// The cell-shift table of the mixed force and density passes: the block's own copy in shared
+// memory, or (GBMD_SHIFTS_GLOBAL) the system's copy in global memory, read through L1 and
+// leaving the shared-memory carve-out to L1 (the host writes the same values, D.shift_tab).
+#ifndef GBMD_SHIFTS_GLOBAL
+#define GBMD_SHIFTS_GLOBAL 0
+#endif
+#if GBMD_SHIFTS_GLOBAL
+#define SHIFT_TABLE(name) const float4* __restrict__ name = D.shift_tab + (long long)s * 128
+#else
+#define SHIFT_TABLE(name)   \
+  __shared__ float4 name[125]; \
+  load_shifts(S, name)
+#endif
+
 // Epilogue shared by the force kernels: turns the total force on atom i into its acceleration
 // (a = F * forcefactor/m, liblpmd/simulation/pairpotential.cc:62), applies fixedvel, and unless
 // EPI_FORCES advances the velocity: v = v + (0.5*dt) * (a_old + a) (plugins/velocityverlet.cc:73-74).
@@ -470,9 +484,10 @@ __device__ __forceinline__ void warp_list_prefetch2(const Dev& D, const SysDev& 
 // How the mixed force and density passes read their list rows (template parameter FEED, chosen
 // per launch): FEED_REGS, each lane loads its own entries into registers with L1-bypassing loads;
 // FEED_RING, bulk asynchronous copies into a per-warp shared-memory ring.  Results are bitwise
-// the same.  Measured on the GB300: single large systems run 1.6-1.8 % faster with registers
-// (without the ring's shared memory the L1 that serves the neighbour gathers is 32 KB larger
-// per SM), the 512-system LJ ensemble 2.6 % faster with the ring.
+// the same.  Measured on the GB300: the single 495k copper system runs 1.5 % faster with
+// registers (without the ring's shared memory the L1 that serves the neighbour gathers is 32 KB
+// larger per SM), the single 256k LJ liquid 0.4 % and the 512-system LJ ensemble 2.6 % faster
+// with the ring.
 constexpr int FEED_REGS = 0, FEED_RING = 1;
 
 // Tile of a block of the mixed force and density passes: blockIdx.x, or with GBMD_SM_TILES=1 a
@@ -525,14 +540,13 @@ __device__ __forceinline__ void release_tile(const Dev& D) {
 
 template <int PC, int SPECIES, int SCN, int SCM, int FEED>
 __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, const StepParams& sp, const int tile) {
-  __shared__ float4 shifts[125];
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   if (!S.active) {  // whole block: one tile belongs to one system
     if (sp.epi == EPI_KICK_DRIFT && sp.last) hold_tile(D, S, tile, true);
     return;
   }
-  load_shifts(S, shifts);
+  SHIFT_TABLE(shifts);
   const ShiftCorr corr = shift_corr(S);
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;  // index within the system
   const long long i = S.atom_base + li;
@@ -1038,13 +1052,12 @@ __global__ void __launch_bounds__(TILE, GBMD_FORCE_MIN_BLOCKS) k_force32_lanes(D
 // density; cutoff decisions in the guard band re-done in FP64 as in the force kernel.
 template <int SCM, int FEED>
 __device__ __forceinline__ void density32_tile(const Dev& D, const PotParams& P, const int tile) {
-  __shared__ float4 shifts[125];
   __shared__ __align__(16) uint4 ring_s[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar_s[TILE / 32][RING];
   const int s = D.tile_sys[tile];
   const SysDev& S = D.sysd[s];
   if (!S.active) return;  // whole block: one tile belongs to one system
-  load_shifts(S, shifts);
+  SHIFT_TABLE(shifts);
   const ShiftCorr corr = shift_corr(S);
   const int li = D.tile_first[tile] - (int)S.atom_base + (int)threadIdx.x;
   const long long i = S.atom_base + li;

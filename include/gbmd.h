@@ -37,8 +37,9 @@ typedef int gbmd_status;
 
 /* Arithmetic of the force path. */
 #define GBMD_PRECISION_FP64 0  /* FP64 pair maths and accumulation (the reference's)        */
-#define GBMD_PRECISION_MIXED 1 /* FP32 pair maths, int64 fixed-point force/density sums,
-                                  FP64 integration, embedding and global reductions        */
+#define GBMD_PRECISION_MIXED 1 /* FP32 pair maths, int64 fixed-point force/density/energy/
+                                  virial sums, FP64 integration, embedding and global
+                                  reductions                                                */
 
 /* Per-atom flags: the "fixedvel" and "fixedpos" atom tags honoured by
  * TwoStepIntegrator::Advance (liblpmd/simulation/twostepintegrator.cc:20-41). */

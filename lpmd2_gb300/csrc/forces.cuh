@@ -566,9 +566,10 @@ __device__ __forceinline__ void force32_tile(const Dev& D, const PotParams& P, c
   unsigned rechecks = 0;
   bool bad = false;
   // Each warp streams its 32 atoms' list groups (32 x 16 bytes, contiguous for a fixed group
-  // index) through its own ring of shared-memory stages, filled by bulk asynchronous copies
-  // (TMA engine) that run RING groups ahead of the force evaluation.  Warps never wait on
-  // each other inside the loop.
+  // index), with FEED_RING through its own ring of shared-memory stages filled by bulk
+  // asynchronous copies (TMA engine) that run RING groups ahead of the force evaluation, with
+  // FEED_REGS through registers loaded two groups ahead.  Warps never wait on each other
+  // inside the loop.
   __shared__ __align__(16) uint4 ring[TILE / 32][RING][32];
   __shared__ __align__(8) unsigned long long bar[TILE / 32][RING];
   {
